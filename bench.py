@@ -1,0 +1,367 @@
+"""Benchmark of the quasi-static level-set inner loop on GB300.
+
+Workload (the 512^3 throughput configuration): a seeded grain pack on a
+512^3 fill box (3 ghost layers, dx = 0.04), grain radii lognormal
+(mu = ln 8, sigma = 0.3) voxels, porosity 0.30, contact angle 40 degrees,
+so the variable-coefficient model runs with HJ-WENO5 in space and TVD-RK3 in
+time.  One benchmark step is one full inner pseudo-time step of
+constCurvModel3d: CFL estimate, three fused RHS + RK stage kernels, the
+ghost-layer boundary condition after each stage and the three mask
+impositions, over every fill-box voxel.  Metric: voxel-step updates per
+second (fill-box voxels x inner steps / time).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--n 512]
+
+--impl gb300 (default) times the GB300 library: `value` with the arrays
+resident in HBM (CUDA events on the library's stream), `e2e` through the
+reference's C entry point constCurvModel3d with host arrays (host<->device
+copies, trapping, reinitialisation and the volume integrals included).
+--impl reference times the reference algorithm on the host cores (the CPU
+oracle: the reference's drivers and restated kernels, OpenMP over all
+cores) on a bounded z-slab of the same workload.
+For N > 1 (torchrun) every rank advances its own independent volume:
+the path has no exchange between volumes ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lsmpqs-1.0_gb300")
+sys.path.insert(0, PKG)
+
+import qssgpu as Q  # noqa: E402
+import synthetic as S  # noqa: E402
+
+METRIC = "voxel-step updates/s (512^3 FP64, WENO5 + TVD-RK3)"
+UNIT = "voxel-steps/s"
+THETA_DEG = 40.0
+SEED = 512
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for independent replicas (gloo on the host)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_info()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.ws)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def make_workload(n: int, nz: int | None = None):
+    """Mask and initial level set of the grain pack (numpy, ghost box)."""
+    nz = nz or n
+    pack = S.lognormal((n, n, nz), mu=math.log(8.0), sigma=0.3, porosity=0.30, seed=SEED)
+    mask = pack.mask()
+    phi = S.initial_phi(mask, (n, n, nz))
+    return mask, phi
+
+
+def set_options(lib, o):
+    o.theta = THETA_DEG * 3.14159 / 180
+    o.order_space_accur = 5
+    o.order_time_accur = 3
+    o.a = 0.05 / 0.04
+    o.b = 0.04
+    o.check_connectivity = 1
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), f"qss_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q_FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# algorithmic FP64 operations of one WENO5 variable-coefficient RHS + RK stage
+# per voxel (+, -, *, /, sqrt each count one; see the design notes):
+# 3 x (16 differences/scalings + 2 x 75 WENO5 side) + 10 Godunov + 5 advection
+# + 72 curvature + 2 sums + 5 RK combination
+FLOP_PER_VOXEL_STAGE = 3 * (16 + 2 * 75) + 10 + 5 + 72 + 2 + 5
+# algorithmic HBM bytes per voxel-step (each array touched once per stage):
+# stage 1 phi + 5 coefficients -> phi1, stage 2 phi1 + phi + 5 coeff -> phi2,
+# stage 3 phi2 + phi + 5 coeff + 3 masks -> phi1, phi
+BYTES_PER_VOXEL_STEP = 8 * ((1 + 5 + 1) + (2 + 5 + 1) + (2 + 5 + 3 + 2))
+
+
+def gpu_arm(args, dist: Dist):
+    lib = Q.load(Q.GPU_LIB)
+    if not lib.qssgpu_device_available():
+        raise RuntimeError("GB300 library: no CUDA device")
+    n = args.n
+    mask, phi = make_workload(n)
+    g = Q.make_grid(lib, n)
+    v = Q.Volume(g)
+    v["mask"][...] = mask
+    v["phi"][...] = phi
+    o = Q.default_options(lib)
+    set_options(lib, o)
+    a0 = o.a
+    if lib.qssgpu_prepare_step(C.byref(o), C.byref(v.p), C.byref(g), a0):
+        Q.check(lib)
+    nvox = n ** 3
+    out = (C.c_double * 4)()
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        lib.qssgpu_time_steps(C.byref(o), C.byref(v.p), C.byref(g), a0, args.warmup, args.steps, out)
+        Q.check(lib)
+    dist.barrier()
+    ms = dist.max(out[0])
+    value = dist.ws * nvox * args.steps / (ms / 1e3)
+    stage_ms = out[1]
+    launches = int(out[2]) * args.steps
+
+    # e2e through the C entry point with host arrays: one outer iteration of
+    # constCurvModel3d whose pseudo-time window holds about `steps` steps
+    e2e = None
+    if args.e2e:
+        w = Q.Volume(g)
+        lib2 = lib
+        for name in ("mask", "phi"):
+            w[name][...] = v[name]
+        o2 = Q.default_options(lib2)
+        set_options(lib2, o2)
+        # coefficients and masks exactly as drain_model3d sets them, on the host arrays
+        from_host = ["phi", "mask", "mask_w", "mask_nw", "normal_velocity", "curvature_coeff",
+                     "external_velocity_x", "external_velocity_y", "external_velocity_z"]
+        _fill_host_coefficients(lib2, o2, w, a0)
+        dt_est = 0.5 / (o2.b_max_over_dx + o2.max_U_over_dx)
+        o2.tplot = args.steps * dt_est * 0.999
+        o2.tmax = o2.tplot * 0.5
+        o2.use_satn_stop = 0
+        dist.barrier()
+        t0 = time.perf_counter()
+        lib2.constCurvModel3d(C.byref(o2), C.byref(w.p), C.byref(g), None)
+        t1 = time.perf_counter()
+        Q.check(lib2)
+        steps_done, outer = C.c_longlong(0), C.c_longlong(0)
+        lib2.qssgpu_call_stats(C.byref(w.p), C.byref(g), C.byref(steps_done), C.byref(outer))
+        wall = dist.max(t1 - t0)
+        npts = g.num_gridpts
+        h2d = 8 * npts * len(from_host)
+        d2h = 8 * npts * 5 + 4 * npts + npts  # phi, phi_next, phi_prev, mask_w, mask_nw, labels, phi_bin
+        e2e = {"value": dist.ws * nvox * steps_done.value / wall, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "inner_steps": steps_done.value, "outer_iterations": outer.value,
+               "wall_s": wall,
+               "note": "one constCurvModel3d call with host arrays: uploads, inner steps, trapping, three "
+                       "reinitialisations, volume integrals, downloads"}
+        lib2.qssgpu_release(C.byref(w.p))
+
+    peaks, kind = measured_peaks()
+    flop_launch = FLOP_PER_VOXEL_STAGE * nvox
+    achieved_tf = flop_launch / (stage_ms / 1e3) / 1e12 if stage_ms > 0 else 0.0
+    fp64_peak = args.fp64_peak
+    bytes_launch = BYTES_PER_VOXEL_STEP / 3 * nvox
+    achieved_gbs = bytes_launch / (stage_ms / 1e3) / 1e9 if stage_ms > 0 else 0.0
+    roofline = {"bound": "fp64", "achieved": round(achieved_tf, 4), "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": round(achieved_tf / fp64_peak, 4) if fp64_peak else None, "traffic": args.traffic,
+                "kernel": "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
+                "peak_source": "FP64 dense peak of GB300 (nominal 1.25 TFLOP/s; no FP64 figure in MEASURED_PEAKS.json)",
+                "hbm": {"achieved": round(achieved_gbs, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                        "frac": round(achieved_gbs / peaks["hbm_gbs"], 4), "peak_kind": kind}}
+    return {"value": value, "ms": ms, "e2e": e2e, "roofline": roofline, "clocks": clk.summary(),
+            "gpu_launches": launches, "stage_ms": stage_ms}
+
+
+def _fill_host_coefficients(lib, o, w, a0):
+    """Fills the host arrays the way drain_model3d does before calling
+    constCurvModel3d (disconnected masks, mask gradient, coefficients)."""
+    g = w.g
+    gp = C.byref(g)
+    lib.initializeDisconnectedMasks(w["mask_w"].ctypes.data_as(Q.c_double_p), gp)
+    lib.initializeDisconnectedMasks(w["mask_nw"].ctypes.data_as(Q.c_double_p), gp)
+    lib.getcentralgrad3dorder2_(Q.dptr(w["mask_x"]), Q.dptr(w["mask_y"]), Q.dptr(w["mask_z"]), *Q.gb_args(g),
+                                Q.dptr(w["mask"]), *Q.gb_args(g), *Q.fb_args(g), Q.dref(g.dx[0]), Q.dref(g.dx[1]),
+                                Q.dref(g.dx[2]))
+    lib.setSpaceDerivFunc(gp, C.byref(o))
+    lib.setThetaOverlap(C.byref(w.p), gp, C.byref(o))
+    lib.getMainInd_new(C.byref(o), C.byref(w.p), gp)
+    bm, um = C.c_double(0), C.c_double(0)
+    lib.setvarcurvadv3d_(Q.dptr(w["mask"]), Q.dptr(w["mask_x"]), Q.dptr(w["mask_y"]), Q.dptr(w["mask_z"]),
+                         Q.dptr(w["curvature_coeff"]), Q.dptr(w["external_velocity_x"]),
+                         Q.dptr(w["external_velocity_y"]), Q.dptr(w["external_velocity_z"]), C.byref(bm),
+                         C.byref(um), Q.dref(o.b), *Q.gb_args(g), *Q.fb_args(g), Q.dref(g.dx[0]))
+    o.b_max_over_dx, o.max_U_over_dx = bm.value, um.value
+    lib.setvarnorm3d_(Q.dptr(w["mask"]), Q.dptr(w["mask_x"]), Q.dptr(w["mask_y"]), Q.dptr(w["mask_z"]),
+                      Q.dptr(w["normal_velocity"]), Q.dref(a0), Q.dref(o.theta), *Q.gb_args(g), *Q.fb_args(g),
+                      Q.dref(g.dx[0]))
+    Q.check(lib)
+
+
+def cpu_arm(args, nz: int, steps: int, warmup: int, threads: int):
+    """The reference algorithm on the host cores (CPU oracle, OpenMP) on a
+    512 x 512 x nz slab of the workload; returns voxel-steps/s and details."""
+    olib = Q.load(os.path.join(ROOT, "oracle", "liboracle.so"))
+    olib.oracle_set_threads(threads)
+    olib.oracle_time_inner_steps.restype = C.c_double
+    olib.oracle_time_inner_steps.argtypes = [C.POINTER(Q.Options), C.POINTER(Q.QSSDataArrays),
+                                             C.POINTER(Q.Grid), C.c_int, C.c_double, C.c_int]
+    n = args.n
+    mask, phi = make_workload(n, nz)
+    g = Q.make_grid(olib, (n, n, nz))
+    w = Q.Volume(g)
+    w["mask"][...] = mask
+    w["phi"][...] = phi
+    o = Q.default_options(olib)
+    set_options(olib, o)
+    _fill_host_coefficients(olib, o, w, o.a)
+    o.tplot = 1e300
+    if warmup:
+        olib.oracle_time_inner_steps(C.byref(o), C.byref(w.p), C.byref(g), 1, o.a, warmup)
+    sec = olib.oracle_time_inner_steps(C.byref(o), C.byref(w.p), C.byref(g), 1, o.a, steps)
+    vox = n * n * nz
+    return {"value": vox * steps / sec, "sec": sec, "sample": f"{n}x{n}x{nz} fill box (a z-slab of the {n}^3 "
+            f"workload), {steps} inner WENO5/TVD-RK3 steps after {warmup} warm-up", "cores": threads}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-cpu", dest="cpu", action="store_false")
+    ap.add_argument("--cpu-nz", type=int, default=64)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--fp64-peak", type=float, default=1.25)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per stage launch from an ncu capture (optional)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, _, local = dist_info()
+    if ws > 1 and args.impl == "gb300":
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)  # one GPU per rank, before CUDA starts
+    dist = Dist()
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        r = cpu_arm(args, args.cpu_nz, args.steps, args.warmup, threads)
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * r["sec"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": f"{args.n}^3 lognormal grain pack, porosity 0.30, theta 40 deg, "
+                                       "WENO5 + TVD-RK3 (sampled on a z-slab)", "n": args.n},
+                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": r["sample"]},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        dist.close()
+        return
+
+    res = gpu_arm(args, dist)
+    cpu = None
+    if dist.rank == 0 and args.cpu:
+        c = cpu_arm(args, args.cpu_nz, args.cpu_steps, 1, threads)
+        cpu = {"value": c["value"], "unit": UNIT, "cores": threads, "kind": "port", "sample": c["sample"]}
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"{args.n}^3 lognormal grain pack (mu=ln 8, sigma=0.3 voxels), porosity 0.30, "
+                                       "theta 40 deg, WENO5 + TVD-RK3, variable coefficients",
+                           "n": args.n, "ghost": 3, "dx": 0.04, "parallelism": f"replicas x{dist.ws}",
+                           "l2": "inputs larger than L2 (each FP64 array 1.1 GB)"},
+                "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "roofline": res["roofline"],
+                "cpu_baseline": cpu, "clocks": res["clocks"]}
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,274 @@
+// qss_state.cu -- device state per QSS_DataArrays, host<->device transfers, errors.
+#include <cstdlib>
+#include <cstring>
+#include <initializer_list>
+#include <mutex>
+#include <unordered_map>
+
+#include "qss_state.h"
+
+namespace qss {
+
+thread_local int CallScope::depth = 0;
+
+namespace {
+int g_err = QSSGPU_OK;
+char g_msg[1024] = "";
+std::mutex g_mu;
+std::unordered_map<const QSS_DataArrays*, DevVolume*> g_table;
+int g_slabs_override = 0;
+}  // namespace
+
+void set_error(int code, const std::string& msg) {
+  g_err = code;
+  snprintf(g_msg, sizeof g_msg, "%s", msg.c_str());
+  fprintf(stderr, "qssgpu error %d: %s\n", code, g_msg);
+}
+
+void clear_error() {
+  g_err = QSSGPU_OK;
+  g_msg[0] = 0;
+}
+
+void ensure_device() {
+  static int state = -1;  // -1 unknown, 0 none, 1 ok
+  if (state == 1) return;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    state = 0;
+    throw Error(QSSGPU_ERR_NO_DEVICE,
+                std::string("no CUDA device available for the GB300 level-set library (") +
+                    (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices") + ")");
+  }
+  state = 1;
+}
+
+Box box_of(const Grid* g) {
+  Box b;
+  b.nx = g->grid_dims_ghostbox[0];
+  b.ny = g->grid_dims_ghostbox[1];
+  b.nz = g->grid_dims_ghostbox[2];
+  b.ilo = g->ilo_fb - g->ilo_gb;
+  b.ihi = g->ihi_fb - g->ilo_gb;
+  b.jlo = g->jlo_fb - g->jlo_gb;
+  b.jhi = g->jhi_fb - g->jlo_gb;
+  b.klo = g->klo_fb - g->klo_gb;
+  b.khi = g->khi_fb - g->klo_gb;
+  return b;
+}
+
+static void check_grid(const Grid* g) {
+  if (!g) throw Error(QSSGPU_ERR_ARG, "Grid is NULL");
+  if (g->num_dims != 3) throw Error(QSSGPU_ERR_UNSUPPORTED, "only 3-D grids run on the GPU path");
+  Box b = box_of(g);
+  if (b.ilo < 3 || b.jlo < 3 || b.klo < 3 || b.nx - 1 - b.ihi < 3 || b.ny - 1 - b.jhi < 3 ||
+      b.nz - 1 - b.khi < 3)
+    throw Error(QSSGPU_ERR_ARG, "the level-set stencils need at least 3 ghost layers on every face");
+  if (b.fbx() < 2 || b.fby() < 2 || b.fbz() < 2)
+    throw Error(QSSGPU_ERR_ARG, "the fill box must span at least 2 cells per axis");
+  if (b.npts() >= (int64_t)INT32_MAX) throw Error(QSSGPU_ERR_ARG, "ghost box exceeds 2^31 points");
+}
+
+int num_slabs_for(const Grid* g) {
+  int t = g_slabs_override;
+  if (t <= 0) {
+    const char* e = getenv("QSSGPU_SLABS");
+    t = e ? atoi(e) : 1;
+  }
+  if (t < 1) t = 1;
+  int ns = g->khi_fb - g->klo_fb + 1;
+  if (t > ns) t = ns;
+  if (t > 1024) t = 1024;
+  return t;
+}
+
+template <class T>
+static void dalloc(T*& ptr, int64_t count) {
+  if (!ptr) QSS_CK(cudaMalloc((void**)&ptr, (size_t)count * sizeof(T)));
+}
+
+static void destroy_volume(DevVolume* v) {
+  cudaStreamSynchronize(v->stream);
+  void* ptrs[] = {v->phi, v->s1, v->s2, v->phi_prev, v->mask, v->mask_w, v->mask_nw, v->mask_disconn,
+                  v->mask_x, v->mask_y, v->mask_z, v->phi_extra, v->vel_n, v->bcoef, v->vx, v->vy,
+                  v->vz, v->scratch, v->r_phi0, v->r_dist, v->r_next, v->contrib, v->labels, v->nsrc,
+                  v->bin, v->rowlast, v->carry, v->red, v->count, v->dscal, v->ctl};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (v->h_ctl) cudaFreeHost(v->h_ctl);
+  if (v->h_scal) cudaFreeHost(v->h_scal);
+  cudaStreamDestroy(v->stream);
+  delete v;
+}
+
+static bool same_box(const Box& a, const Box& b) {
+  return a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.ilo == b.ilo && a.ihi == b.ihi &&
+         a.jlo == b.jlo && a.jhi == b.jhi && a.klo == b.klo && a.khi == b.khi;
+}
+
+DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g) {
+  ensure_device();
+  check_grid(g);
+  std::lock_guard<std::mutex> lk(g_mu);
+  Box b = box_of(g);
+  auto it = g_table.find(p);
+  if (it != g_table.end()) {
+    if (same_box(it->second->box, b)) return *it->second;
+    destroy_volume(it->second);  // the grid changed under the same struct
+    g_table.erase(it);
+  }
+  DevVolume* v = new DevVolume();
+  v->key = p;
+  v->box = b;
+  v->n = b.npts();
+  v->nfb = (int64_t)b.fbx() * b.fby() * b.fbz();
+  const int64_t n = v->n;
+  QSS_CK(cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking));
+  double** reals[] = {&v->phi, &v->s1, &v->s2, &v->phi_prev, &v->mask, &v->mask_w, &v->mask_nw,
+                      &v->mask_disconn, &v->mask_x, &v->mask_y, &v->mask_z, &v->phi_extra,
+                      &v->vel_n, &v->bcoef, &v->vx, &v->vy, &v->vz, &v->scratch,
+                      &v->r_phi0, &v->r_dist, &v->r_next};
+  for (double** r : reals) dalloc(*r, n);
+  dalloc(v->contrib, v->nfb);
+  dalloc(v->labels, n);
+  dalloc(v->nsrc, n);
+  dalloc(v->bin, n);
+  const int64_t rows = (int64_t)b.fby() * b.fbz();
+  dalloc(v->rowlast, rows);
+  dalloc(v->carry, rows);
+  dalloc(v->red, 4);
+  dalloc(v->count, 1);
+  dalloc(v->dscal, 8);
+  dalloc(v->ctl, 1);
+  QSS_CK(cudaMallocHost((void**)&v->h_ctl, sizeof(Ctl)));
+  QSS_CK(cudaMallocHost((void**)&v->h_scal, 8 * sizeof(double)));
+  QSS_CK(cudaMemsetAsync(v->s1, 0, n * sizeof(double), v->stream));
+  QSS_CK(cudaMemsetAsync(v->s2, 0, n * sizeof(double), v->stream));
+  QSS_CK(cudaStreamSynchronize(v->stream));
+  g_table[p] = v;
+  return *v;
+}
+
+void release_volume(const QSS_DataArrays* p) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_table.find(p);
+  if (it == g_table.end()) return;
+  destroy_volume(it->second);
+  g_table.erase(it);
+}
+
+static void* host_ptr(const QSS_DataArrays* p, HostArray a) {
+  switch (a) {
+    case H_PHI: return p->phi;
+    case H_PHI_NEXT: return p->phi_next;
+    case H_PHI_EXTRA: return p->phi_extra;
+    case H_PHI_PREV: return p->phi_prev;
+    case H_MASK: return p->mask;
+    case H_LSE_RHS: return p->lse_rhs;
+    case H_VEL_N: return p->normal_velocity;
+    case H_BCOEF: return p->curvature_coeff;
+    case H_VX: return p->external_velocity_x;
+    case H_VY: return p->external_velocity_y;
+    case H_VZ: return p->external_velocity_z;
+    case H_MASK_X: return p->mask_x;
+    case H_MASK_Y: return p->mask_y;
+    case H_MASK_Z: return p->mask_z;
+    case H_SCRATCH1: return p->scratch1;
+    case H_SCRATCH2: return p->scratch2;
+    case H_CONN: return p->connectivity;
+    case H_BIN: return p->phi_bin;
+    case H_MASK_W: return p->mask_w;
+    case H_MASK_NW: return p->mask_nw;
+    case H_MASK_DISCONN: return p->mask_disconn_init;
+    default: return nullptr;
+  }
+}
+
+static void* dev_ptr(DevVolume& v, HostArray a) {
+  switch (a) {
+    case H_PHI: return v.phi;
+    case H_PHI_NEXT: return v.phi_next_buf == 1 ? v.s1 : v.s2;
+    case H_PHI_EXTRA: return v.phi_extra;
+    case H_PHI_PREV: return v.phi_prev;
+    case H_MASK: return v.mask;
+    case H_VEL_N: return v.vel_n;
+    case H_BCOEF: return v.bcoef;
+    case H_VX: return v.vx;
+    case H_VY: return v.vy;
+    case H_VZ: return v.vz;
+    case H_MASK_X: return v.mask_x;
+    case H_MASK_Y: return v.mask_y;
+    case H_MASK_Z: return v.mask_z;
+    case H_CONN: return v.labels;
+    case H_BIN: return v.bin;
+    case H_MASK_W: return v.mask_w;
+    case H_MASK_NW: return v.mask_nw;
+    case H_MASK_DISCONN: return v.mask_disconn;
+    default: return nullptr;  // lse_rhs, scratch1/2 have no device copy
+  }
+}
+
+static size_t elem_size(HostArray a) {
+  if (a == H_CONN) return sizeof(int);
+  if (a == H_BIN) return 1;
+  return sizeof(double);
+}
+
+static bool usable(const void* h) {
+  return h != nullptr && h != (const void*)(intptr_t)-1;
+}
+
+void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which) {
+  void* h = host_ptr(p, which);
+  void* d = dev_ptr(v, which);
+  if (!usable(h) || !d) throw Error(QSSGPU_ERR_ARG, "input array is not allocated");
+  QSS_CK(cudaMemcpyAsync(d, h, (size_t)v.n * elem_size(which), cudaMemcpyHostToDevice, v.stream));
+}
+
+void download_dirty(DevVolume& v, QSS_DataArrays* p) {
+  for (int a = 0; a < H_COUNT; a++) {
+    HostArray w = (HostArray)a;
+    void* h = host_ptr(p, w);
+    if (!usable(h)) {
+      v.dirty[a] = v.zero_on_return[a] = false;
+      continue;
+    }
+    if (v.zero_on_return[a]) {
+      QSS_CK(cudaStreamSynchronize(v.stream));
+      memset(h, 0, (size_t)v.n * elem_size(w));
+    } else if (v.dirty[a]) {
+      void* d = dev_ptr(v, w);
+      if (d) QSS_CK(cudaMemcpyAsync(h, d, (size_t)v.n * elem_size(w), cudaMemcpyDeviceToHost, v.stream));
+    }
+    v.dirty[a] = v.zero_on_return[a] = false;
+  }
+  QSS_CK(cudaStreamSynchronize(v.stream));
+}
+
+}  // namespace qss
+
+using namespace qss;
+
+extern "C" {
+
+int qssgpu_last_error(void) { return g_err; }
+const char* qssgpu_error_string(void) { return g_msg; }
+void qssgpu_clear_error(void) { clear_error(); }
+
+void qssgpu_set_slabs(int nslabs) { g_slabs_override = nslabs; }
+
+int qssgpu_get_slabs(const Grid* g) { return g ? num_slabs_for(g) : g_slabs_override; }
+
+void qssgpu_release(QSS_DataArrays* p) { release_volume(p); }
+
+int qssgpu_device_available(void) {
+  try {
+    ensure_device();
+    return 1;
+  } catch (const Error&) {
+    return 0;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,105 @@
+// qss_state.h -- device mirror of one QSS_DataArrays and shared host helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/lsmpqs_types.h"
+#include "qss_kernels.cuh"
+
+namespace qss {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// error codes reported by qssgpu_last_error()
+enum {
+  QSSGPU_OK = 0,
+  QSSGPU_ERR_CUDA = 1,
+  QSSGPU_ERR_NO_DEVICE = 2,
+  QSSGPU_ERR_ARG = 3,
+  QSSGPU_ERR_UNSUPPORTED = 4,
+  QSSGPU_ERR_DEVICE_CHECK = 5,
+};
+
+void set_error(int code, const std::string& msg);
+void clear_error();
+
+#define QSS_CK(expr)                                                                            \
+  do {                                                                                          \
+    cudaError_t e_ = (expr);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw ::qss::Error(::qss::QSSGPU_ERR_CUDA,                                                \
+                         std::string(#expr) + ": " + cudaGetErrorString(e_));                   \
+  } while (0)
+
+void ensure_device();
+
+// Box of a Grid (ghost box origin 0, as every lsmpqs grid has)
+Box box_of(const Grid* g);
+
+// Identity of the host arrays of QSS_DataArrays, used to track which host
+// arrays must be refreshed from the device when a top-level call returns.
+enum HostArray {
+  H_PHI, H_PHI_NEXT, H_PHI_EXTRA, H_PHI_PREV, H_MASK, H_LSE_RHS, H_VEL_N, H_BCOEF, H_VX, H_VY, H_VZ,
+  H_MASK_X, H_MASK_Y, H_MASK_Z, H_SCRATCH1, H_SCRATCH2, H_CONN, H_BIN, H_MASK_W, H_MASK_NW,
+  H_MASK_DISCONN, H_COUNT
+};
+
+struct DevVolume {
+  const QSS_DataArrays* key = nullptr;
+  Box box{};
+  int64_t n = 0;
+  int64_t nfb = 0;
+  cudaStream_t stream = nullptr;
+  // level set and the two stage buffers
+  double *phi = nullptr, *s1 = nullptr, *s2 = nullptr, *phi_prev = nullptr;
+  double *mask = nullptr, *mask_w = nullptr, *mask_nw = nullptr, *mask_disconn = nullptr;
+  double *mask_x = nullptr, *mask_y = nullptr, *mask_z = nullptr, *phi_extra = nullptr;
+  double *vel_n = nullptr, *bcoef = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr;
+  double *scratch = nullptr;                           // trapped-phase work array
+  double *r_phi0 = nullptr, *r_dist = nullptr, *r_next = nullptr;  // reinitialisation
+  double *contrib = nullptr;                           // volume contributions (fill box)
+  int *labels = nullptr, *nsrc = nullptr, *rowlast = nullptr, *carry = nullptr;
+  unsigned char* bin = nullptr;
+  unsigned long long* red = nullptr;  // 4 reduction keys
+  unsigned long long* count = nullptr;
+  double* dscal = nullptr;  // device scalars (volume)
+  Ctl* ctl = nullptr;
+  Ctl* h_ctl = nullptr;  // pinned mirror
+  double* h_scal = nullptr;  // pinned scalars
+  // which stage buffer holds the reference's phi_next
+  int phi_next_buf = 1;
+  // nsrc describes the current vel_n for this many slabs (0 = stale)
+  int nsrc_slabs = 0;
+  unsigned long long nsrc_invalid = 0;
+  // host arrays whose device copy is newer / that must be zero on return
+  bool dirty[H_COUNT] = {};
+  bool zero_on_return[H_COUNT] = {};
+  // statistics of the last top-level call
+  long long inner_steps = 0;
+  long long outer_iters = 0;
+};
+
+DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g);
+void release_volume(const QSS_DataArrays* p);
+
+// host <-> device copies of one array of the struct
+void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which);
+void download_dirty(DevVolume& v, QSS_DataArrays* p);
+
+int num_slabs_for(const Grid* g);
+
+// nesting depth of API calls: only the outermost call moves host data
+struct CallScope {
+  static thread_local int depth;
+  CallScope() { depth++; }
+  ~CallScope() { depth--; }
+  bool outermost() const { return depth == 1; }
+};
+
+}  // namespace qss

@@ -1,0 +1,242 @@
+// qss_uf.cu -- 26-connected component labelling and trapped-phase masks on GB300.
+//
+// The reference labels {phi_bin == 1} with a serial union-find whose union
+// rule always hangs the smaller root under the larger one
+// (src/connectivity/connectivity.c:66-83), so every component ends up named
+// by its LARGEST linear ghost-box index, and background is 0 (:201-214).
+// That label is a property of the component, not of the visiting order, so a
+// concurrent union-find that keeps the same rule (link the smaller root under
+// the larger, by compare-and-swap on the root) produces identical labels:
+//   1. parent[v] = v for every foreground voxel;
+//   2. each voxel unites with its 13 neighbours that precede it in linear
+//      order (the other 13 of the 26 are covered from the other side);
+//   3. labels[v] = root(v), 0 for background.
+// Parent pointers only ever increase along a path (parent[x] > x except at a
+// root), so every walk ends; the walks still carry an iteration cap and set an
+// error flag instead of spinning if the cap is ever reached.
+#include "qss_kernels.cuh"
+
+namespace qss {
+
+namespace {
+
+constexpr int kWalkCap = 1 << 30;
+
+__device__ __forceinline__ int find_root(int* parent, int x, int* err) {
+  int r = x;
+  int it = 0;
+  while (true) {
+    int p = __ldcg(parent + r);  // L2-coherent read: other blocks hook roots concurrently
+    if (p == r) break;
+    r = p;
+    if (++it > kWalkCap) {
+      *err |= ERR_UF_LIMIT;
+      return r;
+    }
+  }
+  // path compression: every node on the walk points to an ancestor
+  int y = x;
+  it = 0;
+  while (y != r && it++ < kWalkCap) {
+    int p = __ldcg(parent + y);
+    if (p == y) break;
+    __stcg(parent + y, r);
+    y = p;
+  }
+  return r;
+}
+
+__device__ __forceinline__ void unite(int* parent, int a, int b, int* err) {
+  int ra = find_root(parent, a, err);
+  int rb = find_root(parent, b, err);
+  int it = 0;
+  while (ra != rb) {
+    if (ra > rb) {
+      int t = ra;
+      ra = rb;
+      rb = t;
+    }
+    const int old = atomicCAS(&parent[ra], ra, rb);  // hang the smaller root under the larger
+    if (old == ra) return;
+    ra = find_root(parent, old, err);
+    rb = find_root(parent, rb, err);
+    if (++it > kWalkCap) {
+      *err |= ERR_UF_LIMIT;
+      return;
+    }
+  }
+}
+
+__global__ void k_uf_init(int64_t n, const unsigned char* __restrict__ bin, int* parent) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    parent[q] = bin[q] ? (int)q : 0;
+}
+
+__global__ void k_uf_hook(Box b, const unsigned char* __restrict__ bin, int* parent, Ctl* ctl) {
+  const int64_t n = b.npts();
+  int err = 0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    if (!bin[q]) continue;
+    const int i = (int)(q % b.nx);
+    const int64_t r = q / b.nx;
+    const int j = (int)(r % b.ny), k = (int)(r / b.ny);
+    // the 13 neighbours with a smaller linear index
+#pragma unroll
+    for (int m = 0; m < 13; m++) {
+      int di, dj, dk;
+      if (m < 9) {
+        dk = -1;
+        dj = m / 3 - 1;
+        di = m % 3 - 1;
+      } else if (m < 12) {
+        dk = 0;
+        dj = -1;
+        di = m - 10;
+      } else {
+        dk = 0;
+        dj = 0;
+        di = -1;
+      }
+      const int i2 = i + di, j2 = j + dj, k2 = k + dk;
+      if (i2 < 0 || j2 < 0 || k2 < 0 || i2 >= b.nx || j2 >= b.ny) continue;
+      const int64_t q2 = b.idx(i2, j2, k2);
+      if (bin[q2]) unite(parent, (int)q, (int)q2, &err);
+    }
+  }
+  if (err && ctl) atomicOr(&ctl->err, err);
+}
+
+__global__ void k_uf_final(int64_t n, const unsigned char* __restrict__ bin, int* parent, Ctl* ctl) {
+  int err = 0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    if (bin[q]) {
+      int r = (int)q;
+      int it = 0;
+      while (parent[r] != r && it++ < kWalkCap) r = parent[r];
+      if (it > kWalkCap) err |= ERR_UF_LIMIT;
+      parent[q] = r;
+    }
+  }
+  if (err && ctl) atomicOr(&ctl->err, err);
+}
+
+// MERGE_SETS(phi, mask_nw) then phi_bin = phi < 0 (trapComponents.c:167-170)
+__global__ void k_bin_nw(int64_t n, double* phi, const double* __restrict__ mask_nw, unsigned char* bin) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    double m = mask_nw[q];
+    double p = phi[q];
+    if (m > 0) {
+      p = -m;
+      phi[q] = p;
+    }
+    bin[q] = (p < 0.0) ? 1 : 0;
+  }
+}
+
+// inlet / outlet reservoirs of trapComponents.c:175-194 and 257-299
+__global__ void k_set_bin_slab(Box b, unsigned char* bin, int center, int outlet) {
+  const int64_t nxy = (int64_t)b.nx * b.ny;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!outlet) {
+    if (center) {
+      const int k = (int)(0.5 * (b.klo + b.khi)), i = (int)(0.5 * (b.ilo + b.ihi));
+      if (t < b.ny) bin[i + (int64_t)t * b.nx + k * nxy] = 1;
+    } else {
+      const int i = b.ilo - 1;
+      const int64_t cnt = (int64_t)b.fby() * b.fbz();
+      if (t < cnt) {
+        const int j = b.jlo + t % b.fby(), k = b.klo + t / b.fby();
+        bin[i + (int64_t)j * b.nx + k * nxy] = 1;
+      }
+    }
+  } else {
+    if (center) {
+      if (t < nxy) {
+        bin[(int64_t)(b.klo - 1) * nxy + t] = 1;
+        bin[(int64_t)(b.khi + 1) * nxy + t] = 1;
+      }
+      if (t < (int64_t)b.ny * b.nz) {
+        const int j = t % b.ny, k = t / b.ny;
+        bin[(b.ilo - 1) + (int64_t)j * b.nx + k * nxy] = 1;
+        bin[(b.ihi + 1) + (int64_t)j * b.nx + k * nxy] = 1;
+      }
+    } else {
+      const int i = b.ihi + 1;
+      const int64_t cnt = (int64_t)b.fby() * b.fbz();
+      if (t < cnt) {
+        const int j = b.jlo + t % b.fby(), k = b.klo + t / b.fby();
+        bin[i + (int64_t)j * b.nx + k * nxy] = 1;
+      }
+    }
+  }
+}
+
+// trapComponents.c:226-259: disconnected non-wetting mask, then the masked
+// wetting phase in scratch and its binary image
+__global__ void k_trap_nw(int64_t n, const int* __restrict__ labels, int main_idx, const double* __restrict__ phi,
+                          const double* __restrict__ mask, double* mask_nw, double* scratch, unsigned char* bin,
+                          double fill) {
+  const int main_label = labels[main_idx];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int l = labels[q];
+    const bool disc = !(l == main_label || l == 0);
+    const double p = phi[q];
+    const double mnw = (disc && p < 0) ? -p : fill;
+    mask_nw[q] = mnw;
+    double s = -p;
+    const double m = mask[q];
+    s = (m > s) ? m : s;
+    s = (mnw > s) ? mnw : s;
+    scratch[q] = s;
+    bin[q] = (s < 0.0) ? 1 : 0;
+  }
+}
+
+__global__ void k_trap_w(int64_t n, const int* __restrict__ labels, int main_idx, const double* __restrict__ scratch,
+                         double* mask_w, double fill) {
+  const int main_label = labels[main_idx];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int l = labels[q];
+    const bool disc = !(l == main_label || l == 0);
+    const double s = scratch[q];
+    mask_w[q] = (disc && s < 0) ? -s : fill;
+  }
+}
+
+unsigned grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 32) b = 152 * 32;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+void launch_label(cudaStream_t s, const Box& b, const unsigned char* bin, int* labels, Ctl* ctl) {
+  const int64_t n = b.npts();
+  k_uf_init<<<grid_for(n), 256, 0, s>>>(n, bin, labels);
+  k_uf_hook<<<grid_for(n), 256, 0, s>>>(b, bin, labels, ctl);
+  k_uf_final<<<grid_for(n), 256, 0, s>>>(n, bin, labels, ctl);
+}
+
+void launch_bin_nw(cudaStream_t s, int64_t n, double* phi, const double* mask_nw, unsigned char* bin) {
+  k_bin_nw<<<grid_for(n), 256, 0, s>>>(n, phi, mask_nw, bin);
+}
+
+void launch_set_bin_slab(cudaStream_t s, const Box& b, unsigned char* bin, int center_inlet, int outlet) {
+  int64_t cnt = (int64_t)b.nx * b.ny;
+  if ((int64_t)b.ny * b.nz > cnt) cnt = (int64_t)b.ny * b.nz;
+  if ((int64_t)b.fby() * b.fbz() > cnt) cnt = (int64_t)b.fby() * b.fbz();
+  k_set_bin_slab<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(b, bin, center_inlet, outlet);
+}
+
+void launch_trap_nw(cudaStream_t s, int64_t n, const int* labels, int main_idx, const double* phi,
+                    const double* mask, double* mask_nw, double* scratch, unsigned char* bin, double fill) {
+  k_trap_nw<<<grid_for(n), 256, 0, s>>>(n, labels, main_idx, phi, mask, mask_nw, scratch, bin, fill);
+}
+
+void launch_trap_w(cudaStream_t s, int64_t n, const int* labels, int main_idx, const double* scratch,
+                   double* mask_w, double fill) {
+  k_trap_w<<<grid_for(n), 256, 0, s>>>(n, labels, main_idx, scratch, mask_w, fill);
+}
+
+}  // namespace qss
