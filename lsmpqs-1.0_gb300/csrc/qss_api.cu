@@ -223,6 +223,8 @@ double dev_inner_loop(DevVolume& v, const SchemeSel& sc, const Options* o, const
     if (!v.h_ctl->active) break;
     if (max_steps > 0 && v.h_ctl->steps >= max_steps) break;
     const double dt = v.h_ctl->dt;
+    // a non-positive or NaN step would never reach tplot (the reference loops forever)
+    if (!(dt > 0)) throw Error(QSSGPU_ERR_ARG, "the CFL time step is not positive (check b_max_over_dx / max_U_over_dx)");
     double remain = (o->tplot - v.h_ctl->dt_sub) / (dt > 0 ? dt : 1.0);
     if (!(remain >= 0)) remain = 1;
     batch = (int)std::min(256.0, remain + 2.0);

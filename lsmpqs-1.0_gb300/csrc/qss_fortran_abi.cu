@@ -413,6 +413,8 @@ void imposemaskparallel_(double* phi_masked, const double* mask, const double* p
   Bounds g = GB;
   Bounds fb = g;
   Box bx = make_box(g, fb);
+  if (*cur_klo_gb < 0 || *cur_khi_gb >= bx.nz)
+    throw Error(QSSGPU_ERR_ARG, "imposemaskparallel: z range outside the ghost box");
   const size_t bytes = (size_t)bx.npts() * sizeof(double);
   DBuf dout(bytes), dm(bytes), dp(bytes);
   h2d(dout, phi_masked, bytes);

@@ -11,16 +11,19 @@
 //   2. each voxel unites with its 13 neighbours that precede it in linear
 //      order (the other 13 of the 26 are covered from the other side);
 //   3. labels[v] = root(v), 0 for background.
-// Parent pointers only ever increase along a path (parent[x] > x except at a
-// root), so every walk ends; the walks still carry an iteration cap and set an
-// error flag instead of spinning if the cap is ever reached.
+// Every write to parent[] increases it (hooking a root under a larger root,
+// or compressing a node to a larger ancestor), so parent[x] > x holds for
+// every non-root, the pointer graph has no cycle and every walk ends; the
+// walks still carry an iteration cap and set an error flag instead of
+// spinning if the cap is ever reached.
 #include "qss_kernels.cuh"
 
 namespace qss {
 
 namespace {
 
-constexpr int kWalkCap = 1 << 30;
+// longest pointer walk tolerated before a device-side error is flagged
+constexpr int kWalkCap = 1 << 22;
 
 __device__ __forceinline__ int find_root(int* parent, int x, int* err) {
   int r = x;
@@ -34,13 +37,14 @@ __device__ __forceinline__ int find_root(int* parent, int x, int* err) {
       return r;
     }
   }
-  // path compression: every node on the walk points to an ancestor
+  // Path compression.  Only nodes below r are rewritten, and only upwards:
+  // another thread may already have moved a node of this path above r, and
+  // lowering it again (or walking past r) could close a cycle.
   int y = x;
   it = 0;
-  while (y != r && it++ < kWalkCap) {
-    int p = __ldcg(parent + y);
-    if (p == y) break;
-    __stcg(parent + y, r);
+  while (y < r && it++ < kWalkCap) {
+    const int p = __ldcg(parent + y);
+    if (p < r) __stcg(parent + y, r);
     y = p;
   }
   return r;
