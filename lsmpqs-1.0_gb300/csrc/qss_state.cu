@@ -215,6 +215,17 @@ static size_t elem_size(HostArray a) {
   return sizeof(double);
 }
 
+// arrays the reference only ever writes on the fill box (mask gradient,
+// model coefficients, trapped-velocity zeroing)
+static bool fill_box_only(HostArray a) {
+  switch (a) {
+    case H_MASK_X: case H_MASK_Y: case H_MASK_Z: case H_VEL_N: case H_BCOEF: case H_VX: case H_VY: case H_VZ:
+      return true;
+    default:
+      return false;
+  }
+}
+
 static bool usable(const void* h) {
   return h != nullptr && h != (const void*)(intptr_t)-1;
 }
@@ -239,7 +250,21 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
       memset(h, 0, (size_t)v.n * elem_size(w));
     } else if (v.dirty[a]) {
       void* d = dev_ptr(v, w);
-      if (d) QSS_CK(cudaMemcpyAsync(h, d, (size_t)v.n * elem_size(w), cudaMemcpyDeviceToHost, v.stream));
+      if (!d) continue;
+      if (fill_box_only(w)) {
+        // the reference writes these arrays on the fill box only: the caller's
+        // ghost values must survive, so only fill-box rows travel
+        const Box& b = v.box;
+        const size_t pitch = (size_t)b.nx * sizeof(double);
+        for (int k = b.klo; k <= b.khi; k++) {
+          const size_t off = (size_t)b.idx(b.ilo, b.jlo, k) * sizeof(double);
+          QSS_CK(cudaMemcpy2DAsync((char*)h + off, pitch, (const char*)d + off, pitch,
+                                   (size_t)b.fbx() * sizeof(double), (size_t)b.fby(), cudaMemcpyDeviceToHost,
+                                   v.stream));
+        }
+      } else {
+        QSS_CK(cudaMemcpyAsync(h, d, (size_t)v.n * elem_size(w), cudaMemcpyDeviceToHost, v.stream));
+      }
     }
     v.dirty[a] = v.zero_on_return[a] = false;
   }

@@ -167,6 +167,7 @@ def load(path: str) -> C.CDLL:
         "qssgpu_prepare_step": (C.c_int, [P(Options), P(QSSDataArrays), P(Grid), C.c_double]),
         "qssgpu_time_steps": (C.c_int, [P(Options), P(QSSDataArrays), P(Grid), C.c_double, C.c_int, C.c_int,
                                         c_double_p]),
+        "qssgpu_fp64_peak": (C.c_int, [c_double_p]),
         "oracle_set_threads": (None, [C.c_int]),
         "oracle_portable_sin": (C.c_double, [C.c_double]),
         "oracle_portable_cos": (C.c_double, [C.c_double]),

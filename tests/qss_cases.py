@@ -14,6 +14,14 @@ def pack_case(lib, n, seed=0, radius=4.0, porosity=0.4):
     """Grid + Volume holding a sphere-pack mask and the initial level set."""
     g = Q.make_grid(lib, n)
     v = Q.Volume(g)
+    # every array starts with caller data, so a value written where the
+    # reference leaves the caller's data untouched shows up as a difference
+    rng = np.random.default_rng(1000 + seed)
+    for name, arr in v.arrays.items():
+        if arr.dtype == np.float64:
+            arr[...] = rng.uniform(-2.0, 2.0, arr.shape)
+        else:
+            arr[...] = rng.integers(0, 2, arr.shape)
     m = S.overlapping(n, radius_vox=radius, porosity=porosity, seed=seed).mask()
     v["mask"][...] = m
     v["phi"][...] = S.initial_phi(m, n)
