@@ -1,0 +1,228 @@
+/*
+ * lsmpqs_gpu.h -- C-ABI of the GB300 implementation of the lsmpqs
+ * quasi-static level-set path (libqssgpu.so).
+ *
+ * Every function below keeps the name, signature, argument meaning, return
+ * convention and side effects of the reference routine it replaces (cited as
+ * file:line inside the lsmpqs-1.0 source tree), so a C caller of the
+ * reference links against libqssgpu.so unchanged.  QSSLIB_REAL is double.
+ * Arrays are host memory owned by the caller, laid out over the ghost box,
+ * column-major (i fastest).  Inside, the arrays live in HBM between calls of
+ * one top-level entry point; on return the caller's arrays hold exactly what
+ * the reference would have left in them.
+ *
+ * Errors never abort the process: an entry point that fails returns the
+ * reference's failure value where it has one (-1 from constCurvModel3d, 1 from
+ * drainTop) and records a code and message for qssgpu_last_error().
+ */
+#ifndef LSMPQS_GPU_H
+#define LSMPQS_GPU_H
+
+#include <stdio.h>
+
+#include "lsmpqs_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- model drivers (the hot path) ---------------------------- */
+
+/* src/level_set_evolution/drain_top.h:28 -- reads data/grid/mask files, runs
+   drain_model3d, writes data_final; returns 0, or 1 on bad input / GPU error */
+int drainTop(Options *options, char *fname_data_in, char *fname_grid_in, char *fname_mask_in);
+/* src/level_set_evolution/imbibe_top.h (imbibeTop) */
+int imbibeTop(Options *options, char *fname_data_in, char *fname_grid_in, char *fname_mask_in);
+
+/* src/level_set_evolution/drain_model3d.h:31 -- increasing-curvature ladder;
+   writes data_step_<n>(.gz) after every curvature step */
+void drain_model3d(Options *options, QSS_DataArrays *p, Grid *g, FILE *fp_out);
+/* src/level_set_evolution/imbibe_model3d.h -- decreasing-curvature ladder */
+void imbibe_model3d(Options *options, QSS_DataArrays *p, Grid *g, FILE *fp_out);
+
+/* src/level_set_evolution/constCurvModel3d.h:29 -- variable-coefficient model
+   (contact angle > 0); returns the pseudo time reached, or -1 when the
+   non-wetting saturation exceeds vol_frac_max or the phase vanishes */
+QSSLIB_REAL constCurvModel3d(Options *options, QSS_DataArrays *p, Grid *g, FILE *fp_out);
+/* src/level_set_evolution/constCurvModel3d.h:30 -- zero contact angle, scalar a */
+QSSLIB_REAL constCurvModel3dNoVar(Options *options, QSS_DataArrays *p, Grid *g, FILE *fp_out,
+                                  QSSLIB_REAL a);
+
+/* src/connectivity/connectivity.h:27 -- trapped non-wetting / wetting masks */
+void trapComponents_mask(QSS_DataArrays *p, Grid *g, Options *options);
+/* src/connectivity/connectivity.h:23 -- 26-connected labels of phi_bin into
+   connectivity: each component carries its largest linear index, 0 = background */
+void findConnectivity3d(QSS_DataArrays *p, Grid *g);
+/* src/connectivity/connectivity.h -- inlet/outlet reference points (host only) */
+void getMainInd_new(Options *options, QSS_DataArrays *p, Grid *g);
+/* src/reinitialization/reinitialize_top.h:28 -- Russo-Smereka subcell-fix
+   reinitialisation of a host array, tmax_r / (0.5 dx) pseudo-time iterations */
+void reinitializeSubcellFix3d(QSSLIB_REAL *data, Grid *g, Options *options);
+
+/* src/utilities/qss_general_util.h (qss_general_util.c:82-143) -- stores one of
+   this library's getrhs3d* routines in options->space_deriv_func */
+void setSpaceDerivFunc(Grid *g, Options *options);
+/* qss_general_util.c:150-207 -- overlap from the contact angle */
+void setThetaOverlap(QSS_DataArrays *p, Grid *g, Options *options);
+/* qss_general_util.c:422-706 -- signed linear extrapolation into the ghost
+   layers; idx 0..5 one face, 6/7/8 an axis, 9 all faces in x, y, z order */
+void signedLinearExtrapolationBCqss(QSSLIB_REAL *phi, Grid *g, int bdry_location_idx);
+/* qss_general_util.c:711-728 */
+void initializeDisconnectedMasks(QSSLIB_REAL *data, Grid *g);
+/* qss_general_util.c:813-833 -- fills p->phi_extra */
+void createReservoirInlet3d(QSS_DataArrays *p, Grid *g);
+
+/* ---------------- kernel-level entry points (Fortran convention) ---------- */
+/* The reference's Fortran kernels, same symbol names and argument lists
+   (src/spatial_derivatives/qss_spatial_derivatives3d.h:22-32,
+   src/time_integration/qss_tvd_runge_kutta3d.h:27-29,
+   src/reinitialization/qss_reinitialization3d.h:42-45,
+   src/utilities/qss_util3d.h:20-29).  Each call copies its host arrays to the
+   GPU, runs one kernel over the given fill box and copies the outputs back. */
+#define LSMPQS_GB6 const int *, const int *, const int *, const int *, const int *, const int *
+void getrhs3d2ndconst_(const double *phi, const double *vel_n, const double *b, double *max_H_over_dX,
+                       double *lse_rhs, LSMPQS_GB6, LSMPQS_GB6, const double *dx, const double *dy,
+                       const double *dz);
+void getrhs3d3rdconst_(const double *phi, const double *vel_n, const double *b, double *max_H_over_dX,
+                       double *lse_rhs, LSMPQS_GB6, LSMPQS_GB6, const double *dx, const double *dy,
+                       const double *dz);
+void getrhs3d2nd_(const double *phi, const double *vel_n, const double *b, const double *vel_x,
+                  const double *vel_y, const double *vel_z, double *max_H_over_dX, double *lse_rhs,
+                  LSMPQS_GB6, LSMPQS_GB6, const double *dx, const double *dy, const double *dz);
+void getrhs3d3rd_(const double *phi, const double *vel_n, const double *b, const double *vel_x,
+                  const double *vel_y, const double *vel_z, double *max_H_over_dX, double *lse_rhs,
+                  LSMPQS_GB6, LSMPQS_GB6, const double *dx, const double *dy, const double *dz);
+void getrhs3d5th_(const double *phi, const double *vel_n, const double *b, const double *vel_x,
+                  const double *vel_y, const double *vel_z, double *max_H_over_dX, double *lse_rhs,
+                  LSMPQS_GB6, LSMPQS_GB6, const double *dx, const double *dy, const double *dz);
+void getcentralgrad3dorder2_(double *phi_x, double *phi_y, double *phi_z, LSMPQS_GB6, const double *phi,
+                             LSMPQS_GB6, LSMPQS_GB6, const double *dx, const double *dy, const double *dz);
+void signedlinearextrapolation3d_(double *phi, LSMPQS_GB6, LSMPQS_GB6, const int *bdry_location_idx);
+void setvarnorm3d_(const double *mask, const double *mask_x, const double *mask_y, const double *mask_z,
+                   double *var_a, const double *a0, const double *ca, LSMPQS_GB6, LSMPQS_GB6,
+                   const double *dx);
+void setvarnorm3dtheta_(const double *mask, const double *mask_x, const double *mask_y,
+                        const double *mask_z, double *var_a, const double *a0, const double *ca,
+                        LSMPQS_GB6, LSMPQS_GB6, const double *dx);
+void setvarcurvadv3d_(const double *mask, const double *mask_x, const double *mask_y,
+                      const double *mask_z, double *var_b, double *vel_x, double *vel_y, double *vel_z,
+                      double *b_max_over_dx, double *max_U_over_dx, const double *const_b, LSMPQS_GB6,
+                      LSMPQS_GB6, const double *dx);
+void qss3drk1step_(double *u_next, LSMPQS_GB6, const double *u_cur, LSMPQS_GB6, const double *rhs,
+                   LSMPQS_GB6, LSMPQS_GB6, const double *dt);
+void qss3dtvdrk2stage2_(double *u_stage2, LSMPQS_GB6, const double *u_stage1, LSMPQS_GB6,
+                        const double *u_cur, LSMPQS_GB6, const double *rhs, LSMPQS_GB6, LSMPQS_GB6,
+                        const double *dt);
+void qss3dtvdrk3stage3_(double *u_next, LSMPQS_GB6, const double *u_stage2, LSMPQS_GB6,
+                        const double *u_cur, LSMPQS_GB6, const double *rhs, LSMPQS_GB6, LSMPQS_GB6,
+                        const double *dt);
+void qss3dcomputedistanceforsubcellfix_(double *distance0, const double *phi0, LSMPQS_GB6, LSMPQS_GB6,
+                                        const double *dx, const double *dy, const double *dz);
+void qss3dcomputereinitializationeqnrhssubcellfixorder1_(double *reinit_rhs, const double *phi,
+                                                         LSMPQS_GB6, const double *phi0,
+                                                         const double *distance0, LSMPQS_GB6,
+                                                         const double *dx, const double *dy,
+                                                         const double *dz);
+void qss3dmaxnormdifflocal_(double *max_norm_diff, const double *field1, LSMPQS_GB6,
+                            const double *field2, LSMPQS_GB6, LSMPQS_GB6, const double *local_zone);
+void imposemaskparallel_(double *phi_masked, const double *mask, const double *phi,
+                         const double *overlap, LSMPQS_GB6, const int *cur_klo_gb,
+                         const int *cur_khi_gb);
+void qss3dvolumeregionphilessthanzero_(double *volume, const double *phi, LSMPQS_GB6, LSMPQS_GB6,
+                                       const double *dx, const double *dy, const double *dz,
+                                       const double *epsilon);
+void imposetrapvelocity3d_(const double *phi_w, const double *phi_nw, double *normal_velocity,
+                           double *curvature_coeff, double *vel_x, double *vel_y, double *vel_z,
+                           LSMPQS_GB6, LSMPQS_GB6, const double *dx);
+#undef LSMPQS_GB6
+
+/* ---------------- data model, options, files (host) ------------------------ */
+/* src/utilities/qss_data_arrays.h:84-182 */
+QSS_DataArrays *allocateQSSDataArrays(void);
+void allocateMemoryForQSSDataArrays(QSS_DataArrays *p, Grid *grid);
+void destroyQSSDataArrays(QSS_DataArrays *p); /* also frees the device copy */
+void writeDataArrayQSS(QSSLIB_REAL *data, Grid *grid, char *file_name, int zip_status);
+void writeDataArrayRaw(QSSLIB_REAL *data, Grid *grid, char *file_name, int zip_status);
+void writeDataArrayUchar(unsigned char *data, Grid *grid, char *file_name, int zip_status);
+void writeDataArrayInt(int *data, Grid *grid, char *file_name, int zip_status);
+void writeDataArrayUcharFB(unsigned char *data, Grid *grid, char *file_name, int zip_status);
+QSSLIB_REAL *readDataArrayQSS(int *grid_dims_ghostbox, char *file_name);
+int *readDataArrayInt(int *grid_dims_ghostbox, char *file_name);
+/* src/geometry/qss_grid.h:103-340 */
+Grid *allocateGrid(void);
+Grid *createGridSetDx(int num_dims, QSSLIB_REAL dx, QSSLIB_REAL *x_lo, QSSLIB_REAL *x_hi,
+                      QSSLIB_SPATIAL_DERIVATIVE_ACCURACY_TYPE accuracy);
+Grid *createGridSetDxDyDz(int num_dims, QSSLIB_REAL dx, QSSLIB_REAL dy, QSSLIB_REAL dz,
+                          QSSLIB_REAL *x_lo, QSSLIB_REAL *x_hi,
+                          QSSLIB_SPATIAL_DERIVATIVE_ACCURACY_TYPE accuracy);
+Grid *createGridSetGridDims(int num_dims, int *grid_dims, QSSLIB_REAL *x_lo, QSSLIB_REAL *x_hi,
+                            QSSLIB_SPATIAL_DERIVATIVE_ACCURACY_TYPE accuracy);
+Grid *copyGrid(Grid *grid);
+void destroyGrid(Grid *grid);
+void printGrid(Grid *grid, FILE *fp);
+void writeGridToAsciiFile(Grid *grid, char *file_name, int zip_status);
+void writeGridToBinaryFile(Grid *grid, char *file_name, int zip_status);
+Grid *readGridFromBinaryFile(char *file_name);
+/* src/utilities/qss_options.h:170-283 */
+Options *allocateOptions(void);
+Options *createOptionsDefault(void);
+Options *createOptionsFromInputFile(char *filename);
+void printOptions(Options *options, FILE *fp);
+void destroyOptions(Options *options);
+/* src/utilities/qss_file.h:30-58 */
+void checkUnzipFile(char *file_name, int *pzip_status, char **pfile_base);
+void zipFile(char *file_base, int zip_status);
+/* src/geometry/qss_initialization3d.h (signed distances, evaluated on the GPU) */
+void createIntersectionOfSpheres(QSSLIB_REAL *phi, int num_spheres, QSSLIB_REAL *center_x,
+                                 QSSLIB_REAL *center_y, QSSLIB_REAL *center_z, QSSLIB_REAL *radius,
+                                 int *inside_flag, Grid *grid);
+void createSphere(QSSLIB_REAL *phi, QSSLIB_REAL center_x, QSSLIB_REAL center_y, QSSLIB_REAL center_z,
+                  QSSLIB_REAL radius, int inside_flag, Grid *grid);
+void createIntersectionOfHalfSpaces3d(QSSLIB_REAL *phi, int num_half_spaces, QSSLIB_REAL *normal_x,
+                                      QSSLIB_REAL *normal_y, QSSLIB_REAL *normal_z,
+                                      QSSLIB_REAL *point_x, QSSLIB_REAL *point_y,
+                                      QSSLIB_REAL *point_z, Grid *grid);
+void createPlane(QSSLIB_REAL *phi, QSSLIB_REAL normal_x, QSSLIB_REAL normal_y, QSSLIB_REAL normal_z,
+                 QSSLIB_REAL point_x, QSSLIB_REAL point_y, QSSLIB_REAL point_z, Grid *grid);
+void createPolyhedron3d(QSSLIB_REAL *phi, int num_planes, QSSLIB_REAL *normal_x,
+                        QSSLIB_REAL *normal_y, QSSLIB_REAL *normal_z, QSSLIB_REAL *point_x,
+                        QSSLIB_REAL *point_y, QSSLIB_REAL *point_z, Grid *grid);
+void createIntersectionOfBoxes(QSSLIB_REAL *phi, int num_cuboids, QSSLIB_REAL *corner_x,
+                               QSSLIB_REAL *corner_y, QSSLIB_REAL *corner_z,
+                               QSSLIB_REAL *side_length_x, QSSLIB_REAL *side_length_y,
+                               QSSLIB_REAL *side_length_z, int *inside_flag, Grid *grid);
+void createBox(QSSLIB_REAL *phi, QSSLIB_REAL corner_x, QSSLIB_REAL corner_y, QSSLIB_REAL corner_z,
+               QSSLIB_REAL side_length_x, QSSLIB_REAL side_length_y, QSSLIB_REAL side_length_z,
+               int inside_flag, Grid *grid);
+
+/* ---------------- GB300 extensions (no counterpart in the reference) ------- */
+/* error state: 0 = no error since the last clear */
+int qssgpu_last_error(void);
+const char *qssgpu_error_string(void);
+void qssgpu_clear_error(void);
+/* 1 if a CUDA device is usable by the library */
+int qssgpu_device_available(void);
+/* Number of z-slabs whose last voxels set the CFL step, i.e. the OpenMP thread
+   count of the reference run to reproduce (default 1, or $QSSGPU_SLABS);
+   0 restores the default */
+void qssgpu_set_slabs(int nslabs);
+int qssgpu_get_slabs(const Grid *g);
+/* frees the device copy kept for p (destroyQSSDataArrays calls it) */
+void qssgpu_release(QSS_DataArrays *p);
+/* inner steps and outer iterations of the last top-level call on p */
+void qssgpu_call_stats(const QSS_DataArrays *p, const Grid *g, long long *inner_steps,
+                       long long *outer_iters);
+/* benchmark support: drain_model3d's set-up for curvature a0 with the arrays
+   left in HBM, then timing of `steps` inner steps after `warmup`
+   (out[0] total ms, out[1] mean ms per stage kernel, out[2] kernels per step,
+   out[3] ms inside stage kernels); FP64 throughput probe (TFLOP/s of DFMA, DADD) */
+int qssgpu_prepare_step(Options *o, QSS_DataArrays *p, Grid *g, double a0);
+int qssgpu_time_steps(Options *o, QSS_DataArrays *p, Grid *g, double a0, int warmup, int steps,
+                      double *out);
+int qssgpu_fp64_peak(double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LSMPQS_GPU_H */

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <initializer_list>
 
+#include "../../include/lsmpqs_gpu.h"
 #include "../../include/lsmpqs_types.h"
 #include "qss_fortran_abi.h"
 

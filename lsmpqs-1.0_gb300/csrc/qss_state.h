@@ -6,6 +6,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "../../include/lsmpqs_gpu.h"
 #include "../../include/lsmpqs_types.h"
 #include "qss_kernels.cuh"
 
