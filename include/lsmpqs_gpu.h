@@ -221,6 +221,26 @@ int qssgpu_time_steps(Options *o, QSS_DataArrays *p, Grid *g, double a0, int war
                       double *out);
 int qssgpu_fp64_peak(double *out);
 
+/* Allocation-free smoothed volume of {phi < 0} (no counterpart in the
+   reference; same result, bit for bit, as qss3dvolumeregionphilessthanzero_).
+   For callers that must not allocate device memory while they run -- a
+   framework that owns all of HBM through its own pool, or code recording a
+   stream capture, where cudaMalloc cannot be recorded -- and that already hold
+   their data on the GPU.  d_phi (the ghost box gb = {0, nx-1, 0, ny-1, 0,
+   nz-1}) and d_volume (one double) are DEVICE pointers of the caller; ib is
+   the summed box; work is queued on `stream` (a cudaStream_t, NULL = default
+   stream) and the result is in *d_volume when the stream reaches it.  The
+   per-voxel contributions live in one fixed device array of 2^21 doubles
+   (16 MiB) that every GPU loading the library holds until the process exits:
+   boxes of more than 2^21 voxels are rejected with QSSGPU_ERR_ARG.  The first
+   call on a device looks up that array's device address (make it before any
+   stream capture).  All calls share the array, which keeps the previous
+   call's contents (each call overwrites what it reads, nothing needs
+   clearing): calls that can overlap on the GPU race.  Returns 0 or an error
+   code (see qssgpu_last_error). */
+int qssgpu_volume_noalloc(const double *d_phi, const int gb[6], const int ib[6], double dx, double dy,
+                          double dz, double epsilon, double *d_volume, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

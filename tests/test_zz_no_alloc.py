@@ -1,0 +1,60 @@
+"""The allocation-free volume entry point, for callers that cannot allocate
+device memory while they run (a framework owning all of HBM through its own
+pool, or code recording a stream capture).  It must return, through device
+pointers, exactly what the allocating entry point returns for the same phi,
+call after call (the fixed scratch array keeps the previous call's data)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import qssgpu as Q
+from qss_cases import pack_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _bind(lib):
+    f = lib.qssgpu_volume_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_double, C.c_double, C.c_double,
+                  C.c_double, C.c_void_p, C.c_void_p]
+    return f
+
+
+def test_volume_noalloc_matches_allocating_entry_point(gpu, oracle):
+    torch = pytest.importorskip("torch")
+    noalloc = _bind(gpu)
+    for n, seed in ((24, 3), (40, 5)):  # two calls in a row, different boxes
+        g, v = pack_case(oracle, n, seed=seed)
+        phi = v["phi"]
+        eps = 1.5 * g.dx[0]
+        want = C.c_double(-1.0)
+        gpu.qss3dvolumeregionphilessthanzero_(C.byref(want), Q.dptr(phi), *Q.gb_args(g), *Q.fb_args(g),
+                                              Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]), Q.dref(eps))
+        Q.check(gpu)
+        d_phi = torch.from_numpy(phi).to("cuda")
+        d_vol = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        gb = (C.c_int * 6)(g.ilo_gb, g.ihi_gb, g.jlo_gb, g.jhi_gb, g.klo_gb, g.khi_gb)
+        ib = (C.c_int * 6)(g.ilo_fb, g.ihi_fb, g.jlo_fb, g.jhi_fb, g.klo_fb, g.khi_fb)
+        rc = noalloc(d_phi.data_ptr(), gb, ib, g.dx[0], g.dx[1], g.dx[2], eps, d_vol.data_ptr(), None)
+        torch.cuda.synchronize()
+        Q.check(gpu)
+        assert rc == 0
+        got = d_vol.item()
+        assert want.value > 0
+        assert got == want.value, (got, want.value)  # bit for bit, the tolerance of every parity test
+
+
+def test_volume_noalloc_rejects_boxes_beyond_its_scratch(gpu):
+    torch = pytest.importorskip("torch")
+    noalloc = _bind(gpu)
+    d = torch.zeros(1, dtype=torch.float64, device="cuda")
+    gb = (C.c_int * 6)(0, 135, 0, 135, 0, 135)
+    ib = (C.c_int * 6)(3, 132, 3, 132, 3, 132)  # 130^3 voxels > 2^21
+    rc = noalloc(d.data_ptr(), gb, ib, 0.04, 0.04, 0.04, 0.06, d.data_ptr(), None)
+    assert rc != 0
+    msg = gpu.qssgpu_error_string().decode()
+    gpu.qssgpu_clear_error()
+    assert "scratch" in msg
