@@ -1,0 +1,83 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every function
+include/lsmpqs_gpu.h declares, and the public structs are laid out exactly as
+the reference's headers lay them out (FP64 build)."""
+import ctypes as C
+import json
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+import qssgpu as Q
+from abi_probe import STRUCTS, probe_source
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+LAYOUT = os.path.join(ROOT, "tests", "golden", "abi_layout.json")
+
+
+def declared_functions():
+    """Function names declared in include/lsmpqs_gpu.h."""
+    src = open(os.path.join(INCLUDE, "lsmpqs_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"#define[^\n]*\n", "\n", src)
+    names = set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", src))
+    return sorted(n for n in names if n not in {"if", "sizeof"} and not n.isupper())
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(Q.GPU_LIB):
+        pytest.fail("libqssgpu.so is not built (run __graft_entry__.build())")
+    return C.CDLL(Q.GPU_LIB)
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) > 60
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+
+
+def test_header_compiles_as_c_and_cxx():
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        with open(src, "w") as f:
+            f.write('#include "lsmpqs_gpu.h"\nint main(void){ return qssgpu_last_error(); }\n')
+        subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I" + INCLUDE, src], check=True)
+        subprocess.run(["g++", "-x", "c++", "-Wall", "-Werror", "-fsyntax-only", "-I" + INCLUDE, src], check=True)
+
+
+def test_struct_layout_matches_reference():
+    with open(LAYOUT) as f:
+        want = json.load(f)
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "p.c")
+        with open(src, "w") as f:
+            f.write(probe_source('#include "lsmpqs_types.h"\n'))
+        exe = os.path.join(d, "p")
+        subprocess.run(["gcc", "-I" + INCLUDE, src, "-o", exe], check=True)
+        got = json.loads(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)
+    assert got == want
+    for cname, cls in STRUCTS.items():  # and the Python binding agrees
+        assert C.sizeof(cls) == want[f"{cname}.sizeof"]
+        for name, *_ in cls._fields_:
+            assert getattr(cls, name).offset == want[f"{cname}.{name}"]
+
+
+def test_no_device_is_reported_not_crashed(lib):
+    """On a machine without a GPU every entry point fails loudly and cleanly."""
+    L = Q.load(Q.GPU_LIB)
+    if L.qssgpu_device_available():
+        pytest.skip("a GPU is present")
+    g = Q.make_grid(L, 8)
+    v = Q.Volume(g)
+    o = Q.default_options(L)
+    L.qssgpu_clear_error()
+    t = L.constCurvModel3d(C.byref(o), C.byref(v.p), C.byref(g), None)
+    assert t == -1
+    assert L.qssgpu_last_error() != 0
+    assert b"CUDA" in L.qssgpu_error_string() or b"device" in L.qssgpu_error_string()
+    L.qssgpu_clear_error()

@@ -1,0 +1,142 @@
+"""Host-side parts of the C API in libqssgpu.so, no GPU needed: the option
+file parser, grid construction and the binary grid / data-array formats.
+Checked against expected values and, where it was built, against the
+reference's own C implementation (oracle/_ref)."""
+import ctypes as C
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+import qssgpu as Q
+
+DECK = """\
+outfile run/out_file
+dx 0.04
+a 0.3
+amax 2.5
+amin 0.2
+b 0.05
+dc 0.5
+tmax 40
+tplot 0.25
+theta 35
+space_accur 5
+time_accur 3
+eps_stop 0.02
+err_check_zone 0.6
+eps_coefficient 1.2
+check_connectivity 1
+checkpoint 1
+center_inlet 0
+reservoir_inlet 0
+mask_reinit 0
+init_step 4
+vol_frac_max 0.9
+use_satn_stop 0
+use_var_theta 0
+overlap 0.01
+save_data 0
+print_details 0
+accuracy very_high
+unknown_key 5
+"""
+
+FIELDS = ["dx", "a", "amax", "amin", "b", "dc", "tmax", "tplot", "theta", "order_space_accur", "order_time_accur",
+          "eps_stop", "err_check_zone", "eps_coefficient", "check_connectivity", "checkpoint", "center_inlet",
+          "reservoir_inlet", "mask_reinit", "init_step", "vol_frac_max", "use_satn_stop", "use_var_theta",
+          "overlap", "save_data", "print_details", "accuracy_id", "tmax_r", "cmax"]
+
+
+@pytest.fixture(scope="module")
+def host():
+    if not os.path.exists(Q.GPU_LIB):
+        pytest.fail("libqssgpu.so is not built")
+    lib = Q.load(Q.GPU_LIB)
+    lib.createOptionsFromInputFile.restype = C.POINTER(Q.Options)
+    lib.createOptionsFromInputFile.argtypes = [C.c_char_p]
+    return lib
+
+
+def _parse(lib, path):
+    f = lib.createOptionsFromInputFile
+    f.restype = C.POINTER(Q.Options)
+    f.argtypes = [C.c_char_p]
+    op = f(path.encode())
+    o = Q.Options()
+    C.pointer(o)[0] = op[0]
+    lib.destroyOptions(op)
+    return o
+
+
+def test_option_file(host, tmp_path):
+    p = tmp_path / "deck"
+    p.write_text(DECK)
+    o = _parse(host, str(p))
+    assert o.outfile == b"run/out_file" and o.path == b"run/"
+    assert (o.a, o.amax, o.amin, o.b, o.dc, o.tmax, o.tplot) == (0.3, 2.5, 0.2, 0.05, 0.5, 40.0, 0.25)
+    assert o.theta == 35 * 3.14159 / 180
+    assert (o.order_space_accur, o.order_time_accur, o.init_step, o.accuracy_id) == (5, 3, 4, 3)
+    assert (o.checkpoint, o.reservoir_inlet, o.mask_reinit, o.save_data, o.print_details) == (1, 0, 0, 0, 0)
+    assert o.tmax_r == 10 * 0.04 and o.err_check_zone == 0.6 and o.overlap == 0.01
+
+
+def test_option_file_matches_reference_parser(host, tmp_path):
+    ref_path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                            "libqss_ref.so")
+    if not os.path.exists(ref_path):
+        pytest.skip("reference C build not present")
+    ref = Q.load(ref_path)
+    p = tmp_path / "deck"
+    p.write_text(DECK)
+    a, b = _parse(host, str(p)), _parse(ref, str(p))
+    for f in FIELDS:
+        assert getattr(a, f) == getattr(b, f), f
+    assert a.outfile == b.outfile and a.path == b.path and a.accuracy == b.accuracy
+
+
+def test_defaults_match_reference_defaults(host):
+    o = Q.default_options(host)
+    assert (o.dx, o.tmax, o.tplot, o.a, o.b, o.eps_stop, o.dc, o.amax, o.amin) == \
+        (0.04, 150.0, 0.5, 0.15, 0.04, 0.014, 0.1, 10.0, 0.05)
+    assert (o.order_space_accur, o.order_time_accur, o.check_connectivity, o.use_satn_stop) == (3, 3, 1, 1)
+    assert o.err_check_zone == 20 * 0.04 and o.vol_frac_max == 0.97 and o.eps_coefficient == 1.5
+
+
+@pytest.mark.parametrize("acc", [0, 1, 2, 3])
+def test_grid_and_files(host, oracle, tmp_path, acc):
+    dims = (C.c_int * 3)(12, 9, 7)
+    lo = (C.c_double * 3)(0.12, 0.12, 0.12)
+    hi = (C.c_double * 3)(0.12 + 12 * 0.04, 0.12 + 9 * 0.04, 0.12 + 7 * 0.04)
+    gh = host.createGridSetGridDims(3, dims, lo, hi, acc)
+    go = oracle.createGridSetGridDims(3, dims, lo, hi, acc)
+    assert bytes(C.string_at(gh, C.sizeof(Q.Grid))) == bytes(C.string_at(go, C.sizeof(Q.Grid)))
+    g = gh[0]
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        host.writeGridToBinaryFile(gh, b"grid", 1)
+        f = host.readGridFromBinaryFile
+        f.restype = C.POINTER(Q.Grid)
+        f.argtypes = [C.c_char_p]
+        g2 = f(b"grid.gz")
+        assert bytes(C.string_at(g2, C.sizeof(Q.Grid))) == bytes(C.string_at(gh, C.sizeof(Q.Grid)))
+        n = g.num_gridpts
+        data = np.random.default_rng(acc).standard_normal(n)
+        host.writeDataArrayQSS.argtypes = [Q.c_double_p, C.POINTER(Q.Grid), C.c_char_p, C.c_int]
+        host.writeDataArrayQSS(Q.dptr(data), gh, b"arr", 1)
+        with gzip.open("arr.gz", "rb") as fh:
+            raw = fh.read()
+        dims3 = np.frombuffer(raw[:12], dtype=np.int32)
+        assert list(dims3) == list(g.grid_dims_ghostbox)
+        assert np.array_equal(np.frombuffer(raw[12:], dtype=np.float64), data)
+        rd = host.readDataArrayQSS
+        rd.restype = Q.c_double_p
+        rd.argtypes = [C.POINTER(C.c_int), C.c_char_p]
+        d3 = (C.c_int * 3)()
+        back = rd(d3, b"arr.gz")
+        assert list(d3) == list(g.grid_dims_ghostbox)
+        assert np.array_equal(np.ctypeslib.as_array(back, (n,)), data)
+    finally:
+        os.chdir(cwd)
