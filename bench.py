@@ -163,11 +163,22 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-# algorithmic FP64 operations of one WENO5 variable-coefficient RHS + RK stage
-# per voxel (+, -, *, /, sqrt each count one; see the design notes):
-# 3 x (16 differences/scalings + 2 x 75 WENO5 side) + 10 Godunov + 5 advection
-# + 72 curvature + 2 sums + 5 RK combination
-FLOP_PER_VOXEL_STAGE = 3 * (16 + 2 * 75) + 10 + 5 + 72 + 2 + 5
+# Algorithmic FP64 operations per voxel (+, -, *, /, sqrt each count one;
+# max/min of squares are integer compares) of each stage kernel:
+#   fused stage kernel: 3 x (16 differences/scalings + 2 x 75 WENO5 side)
+#     + 10 Godunov + 5 advection + 72 curvature + 2 sums + 5 RK combination;
+#   one WENO5 axis pass with shared sub-expressions: 9 per face (difference,
+#     scaling, square, 6 scaled copies) + 35 per centre (smoothness terms)
+#     + 2 eps + 2 x 26 per side (3 candidates, weights, combination);
+#   combine: 10 Godunov + 5 advection + 72 curvature + 2 sums + 5 RK.
+FLOP_PER_VOXEL = {0: 3 * (16 + 2 * 75) + 10 + 5 + 72 + 2 + 5,
+                  1: 9 + 35 + 2 + 2 * 26, 2: 9 + 35 + 2 + 2 * 26, 3: 9 + 35 + 2 + 2 * 26,
+                  4: 10 + 5 + 72 + 2 + 5}
+KERNEL_NAME = {0: "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
+               1: "k_weno_axis<0> (WENO5 x-pass, shared sub-expressions)",
+               2: "k_weno_axis<1> (WENO5 y-pass, shared sub-expressions)",
+               3: "k_weno_axis<2> (WENO5 z-pass, shared sub-expressions)",
+               4: "k_weno_combine (Godunov + advection + curvature + TVD-RK)"}
 # algorithmic HBM bytes per voxel-step (each array touched once per stage):
 # stage 1 phi + 5 coefficients -> phi1, stage 2 phi1 + phi + 5 coeff -> phi2,
 # stage 3 phi2 + phi + 5 coeff + 3 masks -> phi1, phi
@@ -190,7 +201,7 @@ def gpu_arm(args, dist: Dist):
     if lib.qssgpu_prepare_step(C.byref(o), C.byref(v.p), C.byref(g), a0):
         Q.check(lib)
     nvox = n ** 3
-    out = (C.c_double * 4)()
+    out = (C.c_double * 15)()
     dist.barrier()
     with ClockSampler(dist.local) as clk:
         lib.qssgpu_time_steps(C.byref(o), C.byref(v.p), C.byref(g), a0, args.warmup, args.steps, out)
@@ -198,7 +209,11 @@ def gpu_arm(args, dist: Dist):
     dist.barrier()
     ms = dist.max(out[0])
     value = dist.ws * nvox * args.steps / (ms / 1e3)
-    stage_ms = out[1]
+    top = int(out[4])
+    top_ms = out[1]
+    kinds = {KERNEL_NAME[k].split(" ")[0]: {"ms_total": round(out[5 + k], 3), "launches": int(out[10 + k]),
+                                            "share_of_step": round(out[5 + k] / ms, 4) if ms else None}
+             for k in range(5) if out[10 + k] > 0}
     launches = int(out[2]) * args.steps
 
     # e2e through the C entry point with host arrays: one outer iteration of
@@ -244,18 +259,20 @@ def gpu_arm(args, dist: Dist):
         fp64_peak = round(probe[0], 4)
         peak_src = (f"measured by the repo's DFMA probe (8 chains/thread); DADD rate {probe[1]:.3f} TFLOP/s; "
                     "no FP64 figure in MEASURED_PEAKS.json")
-    flop_launch = FLOP_PER_VOXEL_STAGE * nvox
-    achieved_tf = flop_launch / (stage_ms / 1e3) / 1e12 if stage_ms > 0 else 0.0
-    bytes_launch = BYTES_PER_VOXEL_STEP / 3 * nvox
-    achieved_gbs = bytes_launch / (stage_ms / 1e3) / 1e9 if stage_ms > 0 else 0.0
+    flop_launch = FLOP_PER_VOXEL[top] * nvox
+    achieved_tf = flop_launch / (top_ms / 1e3) / 1e12 if top_ms > 0 else 0.0
+    # HBM: the step's algorithmic bytes over the time of all its stage kernels
+    stage_total_ms = out[3] / args.steps
+    achieved_gbs = BYTES_PER_VOXEL_STEP * nvox / (stage_total_ms / 1e3) / 1e9 if stage_total_ms > 0 else 0.0
     roofline = {"bound": "fp64", "achieved": round(achieved_tf, 4), "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": round(achieved_tf / fp64_peak, 4) if fp64_peak else None, "traffic": args.traffic,
-                "kernel": "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
+                "kernel": KERNEL_NAME[top], "flop_per_voxel": FLOP_PER_VOXEL[top],
+                "launch_ms": round(top_ms, 4), "kernels": kinds,
                 "peak_source": peak_src,
                 "hbm": {"achieved": round(achieved_gbs, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                         "frac": round(achieved_gbs / peaks["hbm_gbs"], 4), "peak_kind": kind}}
     return {"value": value, "ms": ms, "e2e": e2e, "roofline": roofline, "clocks": clk.summary(),
-            "gpu_launches": launches, "stage_ms": stage_ms}
+            "gpu_launches": launches, "stage_ms": top_ms}
 
 
 def _fill_host_coefficients(lib, o, w, a0):

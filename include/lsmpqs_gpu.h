@@ -206,6 +206,28 @@ int qssgpu_device_available(void);
    count of the reference run to reproduce (default 1, or $QSSGPU_SLABS);
    0 restores the default */
 void qssgpu_set_slabs(int nslabs);
+/* WENO5 variable-coefficient stages as three axis passes + a combine kernel
+   (1, the default) or as one fused kernel per stage (0; also
+   $QSSGPU_WENO_FUSED=1); -1 restores the default; results are identical.
+   Returns the previous mode. */
+int qssgpu_set_weno_split(int mode);
+/* Share of the split WENO5 stage's FP64 arithmetic computed bit-exactly on
+   the integer pipes: 0 none, 1 divisions, power-of-two scalings and
+   comparisons, 2 (default, also $QSSGPU_EMU) level 1 plus part of the
+   products and sums; -1 restores the default.  Results are identical at
+   every level.  Returns the previous level. */
+int qssgpu_set_emu_level(int level);
+/* Device self-test of the integer-pipe FP64 arithmetic against the native
+   instructions on n generated operand pairs: counts[0..7] = mismatches of
+   div, mul, add, sub, scale2, comparisons, max, sqrt; counts[8] = cases run
+   (counts holds 9 values); first = {operation, x, y} of one mismatch (may
+   be NULL). */
+int qssgpu_emu_selftest(long long n, unsigned long long seed, long long *counts, double *first);
+/* Throughput (G operations/s) of native / emulated division, multiplication
+   and addition: out[0..5] = div native, div emulated, mul native, mul
+   emulated, add native, add emulated; out[6] = multiplications with half
+   of the chains native and half emulated (out holds 7 doubles). */
+int qssgpu_op_rates(double *out);
 int qssgpu_get_slabs(const Grid *g);
 /* frees the device copy kept for p (destroyQSSDataArrays calls it) */
 void qssgpu_release(QSS_DataArrays *p);
@@ -214,8 +236,11 @@ void qssgpu_call_stats(const QSS_DataArrays *p, const Grid *g, long long *inner_
                        long long *outer_iters);
 /* benchmark support: drain_model3d's set-up for curvature a0 with the arrays
    left in HBM, then timing of `steps` inner steps after `warmup`
-   (out[0] total ms, out[1] mean ms per stage kernel, out[2] kernels per step,
-   out[3] ms inside stage kernels); FP64 throughput probe (TFLOP/s of DFMA, DADD) */
+   (out[0] total ms, out[1] mean ms per launch of the stage kernel with the
+   largest total time, out[2] kernels per step, out[3] ms inside stage
+   kernels, out[4] kind of that kernel: 0 fused stage, 1/2/3 WENO5 x/y/z
+   pass, 4 WENO5 combine; out[5..9] ms and out[10..14] launches per kind;
+   out holds 15 doubles); FP64 throughput probe (TFLOP/s of DFMA, DADD) */
 int qssgpu_prepare_step(Options *o, QSS_DataArrays *p, Grid *g, double a0);
 int qssgpu_time_steps(Options *o, QSS_DataArrays *p, Grid *g, double a0, int warmup, int steps,
                       double *out);

@@ -154,6 +154,21 @@ double dev_maxnorm(DevVolume& v, const Options* o) {
 // one inner pseudo-time step (constCurvModel3d.c:127-243), predicated on the
 // device loop condition
 
+// one stage: RHS of `in` fused with the TVD-RK combination into `out`; on the
+// last stage also the impositions into phi (in place)
+void enqueue_stage(DevVolume& v, const SchemeSel& sc, const Coef& c, const ImposeArgs& im, int stage, bool fin,
+                   const double* in, double* out, double* phi_new, const Grid* g) {
+  const double dx = g->dx[0], dy = g->dx[1], dz = g->dx[2];
+  if (sc.scheme == WENO5 && sc.var && weno_split()) {
+    launch_weno_axes(v.stream, v.box, in, dx, dy, dz, v.dplus, v.dminus, v.ctl);
+    launch_weno_combine(v.stream, stage, fin, v.box, dx, dy, dz, in, v.phi, out, phi_new, v.dplus, v.dminus, c,
+                        im, v.ctl);
+  } else {
+    launch_stage(v.stream, sc.scheme, sc.var, stage, fin, v.box, dx, dy, dz, in, v.phi, out, phi_new, c, im,
+                 v.ctl);
+  }
+}
+
 void enqueue_step(DevVolume& v, const SchemeSel& sc, const Coef& c, const ImposeArgs& im, int order,
                   int nslabs, const Grid* g) {
   const Box& b = v.box;
@@ -161,28 +176,32 @@ void enqueue_step(DevVolume& v, const SchemeSel& sc, const Coef& c, const Impose
   cudaStream_t s = v.stream;
   launch_dt(s, sc.scheme, sc.var, b, v.phi, c, nslabs, dx, dy, dz, v.ctl);
   if (order <= 1) {
-    launch_stage(s, sc.scheme, sc.var, 1, false, b, dx, dy, dz, v.phi, v.phi, v.s1, nullptr, c, im, v.ctl);
+    enqueue_stage(v, sc, c, im, 1, false, v.phi, v.s1, nullptr, g);
     launch_ghost(s, b, v.s1, nullptr, im, v.ctl);
     launch_impose_region(s, b, v.s1, v.phi, im, v.ctl);
     v.phi_next_buf = 1;
   } else if (order == 2) {
-    launch_stage(s, sc.scheme, sc.var, 1, false, b, dx, dy, dz, v.phi, v.phi, v.s1, nullptr, c, im, v.ctl);
+    enqueue_stage(v, sc, c, im, 1, false, v.phi, v.s1, nullptr, g);
     launch_ghost(s, b, v.s1, nullptr, im, v.ctl);
-    launch_stage(s, sc.scheme, sc.var, 2, true, b, dx, dy, dz, v.s1, v.phi, v.s2, v.phi, c, im, v.ctl);
+    enqueue_stage(v, sc, c, im, 2, true, v.s1, v.s2, v.phi, g);
     launch_ghost(s, b, v.s2, v.phi, im, v.ctl);
     v.phi_next_buf = 2;
   } else {
-    launch_stage(s, sc.scheme, sc.var, 1, false, b, dx, dy, dz, v.phi, v.phi, v.s1, nullptr, c, im, v.ctl);
+    enqueue_stage(v, sc, c, im, 1, false, v.phi, v.s1, nullptr, g);
     launch_ghost(s, b, v.s1, nullptr, im, v.ctl);
-    launch_stage(s, sc.scheme, sc.var, 2, false, b, dx, dy, dz, v.s1, v.phi, v.s2, nullptr, c, im, v.ctl);
+    enqueue_stage(v, sc, c, im, 2, false, v.s1, v.s2, nullptr, g);
     launch_ghost(s, b, v.s2, nullptr, im, v.ctl);
-    launch_stage(s, sc.scheme, sc.var, 3, true, b, dx, dy, dz, v.s2, v.phi, v.s1, v.phi, c, im, v.ctl);
+    enqueue_stage(v, sc, c, im, 3, true, v.s2, v.s1, v.phi, g);
     launch_ghost(s, b, v.s1, v.phi, im, v.ctl);
     v.phi_next_buf = 1;
   }
 }
 
-int kernels_per_step(int order) { return order <= 1 ? 4 : (order == 2 ? 5 : 7); }
+int kernels_per_step(int order, bool split) {
+  const int per_stage = split ? 4 : 1;
+  const int stages = order <= 1 ? 1 : (order == 2 ? 2 : 3);
+  return 1 + stages * (per_stage + 1) + (order <= 1 ? 1 : 0);
+}
 
 // Runs the inner loop to completion; returns dt_sub.
 double dev_inner_loop(DevVolume& v, const SchemeSel& sc, const Options* o, const Grid* g, double a,
@@ -349,7 +368,10 @@ double path_inner_loop(DevVolume& v, Options* o, Grid* g, double a, int max_step
   SchemeSel sc = scheme_of(o);
   return dev_inner_loop(v, sc, o, g, a, max_steps);
 }
-int path_kernels_per_step(int order) { return kernels_per_step(order); }
+int path_kernels_per_step(DevVolume& v, const Options* o) {
+  SchemeSel sc = scheme_of(o);
+  return kernels_per_step(o->order_time_accur, sc.scheme == WENO5 && sc.var && weno_split());
+}
 void path_upload_for_const_curv(DevVolume& v, QSS_DataArrays* p, const Options* o, bool var) {
   upload_for_const_curv(v, p, o, var);
 }

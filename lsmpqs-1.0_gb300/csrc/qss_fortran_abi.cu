@@ -126,7 +126,16 @@ void rhs_entry(int scheme, bool var, const double* phi, const double* vel_n, con
     c.b_const = *b;
   }
   ImposeArgs im{};
-  launch_stage(s, scheme, var, 0, false, bx, dx, dy, dz, dphi.d(), nullptr, drhs.d(), nullptr, c, im, nullptr);
+  if (scheme == WENO5 && var && weno_split()) {
+    DBuf d0(bytes), d1(bytes), d2(bytes), d3(bytes), d4(bytes), d5(bytes);
+    double* const dp[3] = {d0.d(), d1.d(), d2.d()};
+    double* const dm[3] = {d3.d(), d4.d(), d5.d()};
+    launch_weno_axes(s, bx, dphi.d(), dx, dy, dz, dp, dm, nullptr);
+    launch_weno_combine(s, 0, false, bx, dx, dy, dz, dphi.d(), nullptr, drhs.d(), nullptr, dp, dm, c, im, nullptr);
+    QSS_CK(cudaStreamSynchronize(s));
+  } else {
+    launch_stage(s, scheme, var, 0, false, bx, dx, dy, dz, dphi.d(), nullptr, drhs.d(), nullptr, c, im, nullptr);
+  }
   launch_cfl_at(s, scheme, var, bx, dphi.d(), c, bx.ihi, bx.jhi, bx.khi, dx, dy, dz, dh.d());
   d2h(lse_rhs, drhs, bytes);
   double h;

@@ -19,18 +19,6 @@ namespace {
 
 constexpr double kZeroTol = 1.e-5;
 
-__device__ __forceinline__ double impose3(double v, int64_t idx, const ImposeArgs& im) {
-  double t = im.mask[idx] - im.overlap;
-  v = (t > v) ? t : v;
-  if (im.check_conn) {
-    t = im.mask_w[idx] - 0.0;
-    v = (t > v) ? t : v;
-    t = im.mask_nw[idx] - 0.0;
-    v = (t > v) ? t : v;
-  }
-  return v;
-}
-
 inline dim3 fb_grid(const Box& b, dim3 blk) {
   return dim3((b.fbx() + blk.x - 1) / blk.x, (b.fby() + blk.y - 1) / blk.y, (b.fbz() + blk.z - 1) / blk.z);
 }
@@ -750,11 +738,16 @@ __global__ void k_negate(int64_t n, double* a) {
 static const dim3 kBlk3(32, 4, 1);
 
 // stage-kernel timing (host side): event pairs recorded around each launch
+// of a stage kernel on the profiled stream, tagged with the kernel's kind
 namespace {
 struct StageProfiler {
   bool on = false;
   cudaStream_t stream = nullptr;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+  struct Rec {
+    int kind;
+    cudaEvent_t e0, e1;
+  };
+  std::vector<Rec> ev;
 } g_prof;
 }  // namespace
 
@@ -764,21 +757,40 @@ void qss_profile_stage_begin(cudaStream_t s) {
   g_prof.ev.clear();
 }
 
-void qss_profile_stage_end(double* total_ms, int* launches) {
-  double t = 0;
-  for (auto& e : g_prof.ev) {
-    cudaEventSynchronize(e.second);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e.first, e.second);
-    t += ms;
-    cudaEventDestroy(e.first);
-    cudaEventDestroy(e.second);
+void qss_profile_stage_end(double ms[kProfKinds], int launches[kProfKinds]) {
+  for (int k = 0; k < kProfKinds; k++) {
+    ms[k] = 0;
+    launches[k] = 0;
   }
-  *total_ms = t;
-  *launches = (int)g_prof.ev.size();
+  for (auto& e : g_prof.ev) {
+    cudaEventSynchronize(e.e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e.e0, e.e1);
+    ms[e.kind] += t;
+    launches[e.kind]++;
+    cudaEventDestroy(e.e0);
+    cudaEventDestroy(e.e1);
+  }
   g_prof.ev.clear();
   g_prof.on = false;
 }
+
+cudaEvent_t prof_open(cudaStream_t s) {
+  if (!g_prof.on || s != g_prof.stream) return nullptr;
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, s);
+  return e;
+}
+
+void prof_close(cudaStream_t s, cudaEvent_t e0, int kind) {
+  if (!e0) return;
+  cudaEvent_t e1 = nullptr;
+  cudaEventCreate(&e1);
+  cudaEventRecord(e1, s);
+  g_prof.ev.push_back({kind, e0, e1});
+}
+
 static const int kBlk1 = 256;
 
 static unsigned grid1(int64_t n) {
@@ -824,20 +836,11 @@ void launch_stage(cudaStream_t s, int scheme, bool var, int stage, bool final_st
   a.im = im;
   a.ctl = ctl;
   dim3 g = fb_grid(b, kBlk3);
-  const bool prof = g_prof.on && stage != 0 && s == g_prof.stream;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (prof) {
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, s);
-  }
+  cudaEvent_t e0 = stage != 0 ? prof_open(s) : nullptr;
   if (scheme == ENO2) { if (var) stage_dispatch<ENO2, true>(s, stage, final_stage, g, kBlk3, a); else stage_dispatch<ENO2, false>(s, stage, final_stage, g, kBlk3, a); }
   else if (scheme == ENO3) { if (var) stage_dispatch<ENO3, true>(s, stage, final_stage, g, kBlk3, a); else stage_dispatch<ENO3, false>(s, stage, final_stage, g, kBlk3, a); }
   else { if (var) stage_dispatch<WENO5, true>(s, stage, final_stage, g, kBlk3, a); else stage_dispatch<WENO5, false>(s, stage, final_stage, g, kBlk3, a); }
-  if (prof) {
-    cudaEventRecord(e1, s);
-    g_prof.ev.emplace_back(e0, e1);
-  }
+  prof_close(s, e0, kProfStage);
 }
 
 void launch_cfl_at(cudaStream_t s, int scheme, bool var, const Box& b, const double* phi, const Coef& c, int i,

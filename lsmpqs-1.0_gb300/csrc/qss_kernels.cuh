@@ -47,6 +47,21 @@ struct ImposeArgs {
   int check_conn;
 };
 
+#ifdef __CUDACC__
+// the three mask impositions of one voxel (level_set_evolution/constCurvModel3d.c:228-241)
+__device__ __forceinline__ double impose3(double v, int64_t idx, const ImposeArgs& im) {
+  double t = im.mask[idx] - im.overlap;
+  v = (t > v) ? t : v;
+  if (im.check_conn) {
+    t = im.mask_w[idx] - 0.0;
+    v = (t > v) ? t : v;
+    t = im.mask_nw[idx] - 0.0;
+    v = (t > v) ? t : v;
+  }
+  return v;
+}
+#endif
+
 // ---- inner step ---------------------------------------------------------
 // dt kernel: CFL estimate at the last voxel of each of `nslabs` z-slabs of the
 // stage-1 input, dt, loop condition.
@@ -59,6 +74,19 @@ void launch_dt(cudaStream_t s, int scheme, bool var, const Box& b, const double*
 void launch_stage(cudaStream_t s, int scheme, bool var, int stage, bool final_stage, const Box& b,
                   double dx, double dy, double dz, const double* phi_in, const double* u_cur,
                   double* out, double* phi_new, const Coef& c, const ImposeArgs& im, const Ctl* ctl);
+
+// emulation level of the split WENO5 kernels (defined in qss_state.cu)
+int emu_level();
+
+// WENO5 variable-coefficient stage as three axis passes (one-sided
+// derivatives into dp[axis], dm[axis], ghost-box sized) and a combine kernel
+// (qss_weno.cu); same results as launch_stage for scheme WENO5, var = true.
+void launch_weno_axes(cudaStream_t s, const Box& b, const double* phi, double dx, double dy, double dz,
+                      double* const dp[3], double* const dm[3], const Ctl* ctl);
+void launch_weno_combine(cudaStream_t s, int stage, bool final_stage, const Box& b, double dx, double dy, double dz,
+                         const double* phi_in, const double* u_cur, double* out, double* phi_new,
+                         double* const dp[3], double* const dm[3], const Coef& c, const ImposeArgs& im,
+                         const Ctl* ctl);
 
 // CFL estimate of one voxel (for the RHS-only entry points)
 void launch_cfl_at(cudaStream_t s, int scheme, bool var, const Box& b, const double* phi, const Coef& c,
@@ -76,8 +104,13 @@ void launch_face(cudaStream_t s, const Box& b, double* a, int face);
 
 // Optional timing of every stage-kernel launch with CUDA events on the
 // launching stream (used by the benchmark entry point).
+// kinds of profiled kernels: fused stage, WENO5 x / y / z passes, combine
+enum { kProfStage = 0, kProfAxisX = 1, kProfAxisY = 2, kProfAxisZ = 3, kProfCombine = 4, kProfKinds = 5 };
 void qss_profile_stage_begin(cudaStream_t s);
-void qss_profile_stage_end(double* total_ms, int* launches);
+void qss_profile_stage_end(double ms[kProfKinds], int launches[kProfKinds]);
+// event before / after one profiled launch on s (no-ops unless s is profiled)
+cudaEvent_t prof_open(cudaStream_t s);
+void prof_close(cudaStream_t s, cudaEvent_t e0, int kind);
 
 // phi_new = impose(src) over the whole ghost box restricted to z in [klo-3, khi+3]
 void launch_impose_region(cudaStream_t s, const Box& b, const double* src, double* phi_new,

@@ -40,7 +40,7 @@ void path_reinit(DevVolume& v, double*& data, const Grid* g, const Options* o);
 void path_trap(DevVolume& v, const Grid* g, const Options* o);
 double path_const_curv(DevVolume& v, bool var, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp, double a);
 double path_inner_loop(DevVolume& v, Options* o, Grid* g, double a, int max_steps);
-int path_kernels_per_step(int order);
+int path_kernels_per_step(DevVolume& v, const Options* o);
 
 namespace {
 
@@ -426,8 +426,11 @@ int qssgpu_prepare_step(Options* o, QSS_DataArrays* p, Grid* g, double a0) {
 
 // Runs `warmup` then `steps` inner steps on the device-resident volume with
 // CUDA events on the volume's stream.  out[0] = device ms of the timed steps,
-// out[1] = mean ms of one stage-kernel launch, out[2] = kernel launches per
-// step, out[3] = total ms inside stage kernels.
+// out[1] = mean ms of one launch of the kernel with the largest total time,
+// out[2] = kernel launches per step, out[3] = total ms inside the profiled
+// stage kernels, out[4] = kind of that largest kernel (0 fused stage, 1..3
+// WENO5 x/y/z pass, 4 combine), out[5..9] = total ms per kind, out[10..14] =
+// launches per kind.
 int qssgpu_time_steps(Options* o, QSS_DataArrays* p, Grid* g, double a0, int warmup, int steps, double* out) {
   QSS_API_BEGIN
   DevVolume& v = volume_for(p, g);
@@ -445,15 +448,26 @@ int qssgpu_time_steps(Options* o, QSS_DataArrays* p, Grid* g, double a0, int war
   QSS_CK(cudaEventSynchronize(e1));
   float ms = 0;
   QSS_CK(cudaEventElapsedTime(&ms, e0, e1));
-  double stage_ms = 0;
-  int stage_launches = 0;
-  qss_profile_stage_end(&stage_ms, &stage_launches);
+  double kind_ms[kProfKinds];
+  int kind_n[kProfKinds];
+  qss_profile_stage_end(kind_ms, kind_n);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  int top = 0;
+  double total = 0;
+  for (int k = 0; k < kProfKinds; k++) {
+    total += kind_ms[k];
+    if (kind_ms[k] > kind_ms[top]) top = k;
+  }
   out[0] = ms;
-  out[1] = stage_launches ? stage_ms / stage_launches : 0;
-  out[2] = path_kernels_per_step(o->order_time_accur);
-  out[3] = stage_ms;
+  out[1] = kind_n[top] ? kind_ms[top] / kind_n[top] : 0;
+  out[2] = path_kernels_per_step(v, o);
+  out[3] = total;
+  out[4] = top;
+  for (int k = 0; k < kProfKinds; k++) {
+    out[5 + k] = kind_ms[k];
+    out[10 + k] = kind_n[k];
+  }
   return 0;
   QSS_API_END(return 1)
 }

@@ -17,6 +17,8 @@ char g_msg[1024] = "";
 std::mutex g_mu;
 std::unordered_map<const QSS_DataArrays*, DevVolume*> g_table;
 int g_slabs_override = 0;
+int g_weno_split = -1;  // -1: from the environment
+int g_emu_level = -1;   // -1: from the environment
 }  // namespace
 
 void set_error(int code, const std::string& msg) {
@@ -83,6 +85,24 @@ int num_slabs_for(const Grid* g) {
   return t;
 }
 
+bool weno_split() {
+  int m = g_weno_split;
+  if (m < 0) {
+    const char* e = getenv("QSSGPU_WENO_FUSED");
+    m = (e && atoi(e) == 1) ? 0 : 1;
+  }
+  return m != 0;
+}
+
+int emu_level() {
+  int m = g_emu_level;
+  if (m < 0) {
+    const char* e = getenv("QSSGPU_EMU");
+    m = e ? atoi(e) : 2;
+  }
+  return m < 0 ? 0 : (m > 2 ? 2 : m);
+}
+
 template <class T>
 static void dalloc(T*& ptr, int64_t count) {
   if (!ptr) QSS_CK(cudaMalloc((void**)&ptr, (size_t)count * sizeof(T)));
@@ -96,6 +116,10 @@ static void destroy_volume(DevVolume* v) {
                   v->bin, v->rowlast, v->carry, v->red, v->count, v->dscal, v->ctl};
   for (void* q : ptrs)
     if (q) cudaFree(q);
+  for (int d = 0; d < 3; d++) {
+    if (v->dplus[d]) cudaFree(v->dplus[d]);
+    if (v->dminus[d]) cudaFree(v->dminus[d]);
+  }
   if (v->h_ctl) cudaFreeHost(v->h_ctl);
   if (v->h_scal) cudaFreeHost(v->h_scal);
   cudaStreamDestroy(v->stream);
@@ -130,6 +154,10 @@ DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g) {
                       &v->vel_n, &v->bcoef, &v->vx, &v->vy, &v->vz, &v->scratch,
                       &v->r_phi0, &v->r_dist, &v->r_next};
   for (double** r : reals) dalloc(*r, n);
+  for (int d = 0; d < 3; d++) {
+    dalloc(v->dplus[d], n);
+    dalloc(v->dminus[d], n);
+  }
   dalloc(v->contrib, v->nfb);
   dalloc(v->labels, n);
   dalloc(v->nsrc, n);
@@ -282,6 +310,18 @@ const char* qssgpu_error_string(void) { return g_msg; }
 void qssgpu_clear_error(void) { clear_error(); }
 
 void qssgpu_set_slabs(int nslabs) { g_slabs_override = nslabs; }
+
+int qssgpu_set_emu_level(int level) {
+  const int prev = emu_level();
+  g_emu_level = level < 0 ? -1 : (level > 2 ? 2 : level);
+  return prev;
+}
+
+int qssgpu_set_weno_split(int mode) {
+  const int prev = weno_split() ? 1 : 0;
+  g_weno_split = mode < 0 ? -1 : (mode ? 1 : 0);
+  return prev;
+}
 
 int qssgpu_get_slabs(const Grid* g) { return g ? num_slabs_for(g) : g_slabs_override; }
 

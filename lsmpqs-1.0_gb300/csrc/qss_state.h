@@ -65,6 +65,7 @@ struct DevVolume {
   double *scratch = nullptr;                           // trapped-phase work array
   double *r_phi0 = nullptr, *r_dist = nullptr, *r_next = nullptr;  // reinitialisation
   double *contrib = nullptr;                           // volume contributions (fill box)
+  double *dplus[3] = {}, *dminus[3] = {};              // WENO5 one-sided derivatives per axis
   int *labels = nullptr, *nsrc = nullptr, *rowlast = nullptr, *carry = nullptr;
   unsigned char* bin = nullptr;
   unsigned long long* red = nullptr;  // 4 reduction keys
@@ -94,6 +95,15 @@ void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which);
 void download_dirty(DevVolume& v, QSS_DataArrays* p);
 
 int num_slabs_for(const Grid* g);
+// WENO5 variable-coefficient stages as axis passes + combine (true, default)
+// or as the single fused stage kernel ($QSSGPU_WENO_FUSED=1,
+// qssgpu_set_weno_split(0)); both give identical results
+bool weno_split();
+// share of the WENO5 stage's FP64 arithmetic done on the integer pipes
+// (0 none, 1 divisions / power-of-two scalings / comparisons, 2 also part of
+// the products and sums; $QSSGPU_EMU, qssgpu_set_emu_level); all levels give
+// identical results
+int emu_level();
 
 // nesting depth of API calls: only the outermost call moves host data
 struct CallScope {

@@ -1,0 +1,488 @@
+// qss_weno.cu -- WENO5 stage of the variable-coefficient model with shared
+// sub-expressions.
+//
+// The reference evaluates, for every voxel and axis, two WENO5 reconstructions
+// from ten scaled first differences (3d.f:1968-2138).  Most of that work
+// depends only on one cell face or one cell centre and is therefore repeated
+// by up to six neighbouring voxels: the scaled difference v of a face, its
+// square, its multiples by 3 and by the five stencil coefficients, and the
+// smoothness terms of a centre.  Each of those values is an IEEE operation
+// on identical operands wherever it appears, so computing it once per line
+// and reusing it reproduces the reference's values bit for bit while cutting
+// the FP64 instructions per voxel -- the resource that bounds this kernel on
+// GB300 (one FP64 warp instruction per ~64 cycles per scheduler).
+//
+// A stage runs as three axis passes and one combine kernel:
+//   k_weno_axis<AX>: each thread walks a segment of SEG voxels along axis AX
+//     with a sliding window of faces / centres and writes the plus and minus
+//     one-sided derivatives of that axis (2 doubles per voxel);
+//   k_weno_combine: Godunov normal term (with the carried term of voxels whose
+//     speed is below 1e-5), upwind advection, central curvature, TVD-RK
+//     combination and, on the last stage, the three mask impositions.
+// The extra traffic (48 B written + 48 B read per voxel and stage) costs about
+// 2 % of the stage time at 512^3; HBM is idle otherwise.
+//
+// Identities used (v(m) = (phi(m) - phi(m-1)) * inv for face m, c a centre):
+//   plus(i):  v1..v5 = v(i+3), v(i+2), v(i+1), v(i), v(i-1)
+//   minus(i): v1..v5 = v(i-2), v(i-1), v(i),   v(i+1), v(i+2)
+//   A(c) = 13/12((v(c+1) - 2v(c)) + v(c-1))^2   first term of S1+(c-2), S2+(c-1), S3+(c)
+//   B(c) = 13/12((v(c-1) - 2v(c)) + v(c+1))^2   first term of S1-(c+1), S2-(c), S3-(c-1)
+//   E(c) = 1/4 (v(c+1) - v(c-1))^2              second term of S2+(c-1) and S2-(c)
+//   eps-(i) = eps+(i-1)                          (same five squares, max is exact)
+#include "qss_emu.cuh"
+#include "qss_kernels.cuh"
+
+namespace qss {
+
+namespace {
+
+constexpr double k1312 = 13.0 / 12.0;
+constexpr double kC13 = 1.0 / 3.0, kC76 = 7.0 / 6.0, kC116 = 11.0 / 6.0, kC16 = 1.0 / 6.0, kC56 = 5.0 / 6.0;
+constexpr int SEG = 16;  // voxels per thread along the pass axis
+
+// Arithmetic of one emulation level (all levels give identical results):
+//   0: native FP64 instructions only;
+//   1: divisions, square roots, power-of-two scalings and comparisons on the
+//      integer pipes;
+//   2: level 1 plus the products of the curvature numerator in the combine
+//      kernel, which runs with enough warps per scheduler to overlap them with
+//      its FP64 work.  (The axis passes hold ~120 registers per thread, too
+//      few warps to hide the latency of more integer-pipe arithmetic; they run
+//      at level 1 for levels 1 and 2.)
+template <int EMU>
+struct Ar {
+  static __device__ __forceinline__ double div(double a, double b) {
+    if (EMU >= 1) return qss_emu::div(a, b);
+    return a / b;
+  }
+  // x * 2^k
+  static __device__ __forceinline__ double s2(double x, int k) {
+    if (EMU >= 1) return qss_emu::scale2(x, k);
+    return x * (k == 1 ? 2.0 : k == 2 ? 4.0 : k == -2 ? 0.25 : k == -1 ? 0.5 : 1.0);
+  }
+  // products moved at level 2
+  static __device__ __forceinline__ double mul2(double a, double b) {
+    if (EMU >= 2) return qss_emu::mul(a, b);
+    return a * b;
+  }
+};
+
+struct Face {
+  double v, w, t3, c13, c76, c116, c16, c56;
+};
+
+__device__ __forceinline__ Face make_face(double hi, double lo, double inv) {
+  Face f;
+  const double d = hi - lo;
+  f.v = d * inv;
+  f.w = f.v * f.v;
+  f.t3 = 3.0 * f.v;
+  f.c13 = kC13 * f.v;
+  f.c76 = kC76 * f.v;
+  f.c116 = kC116 * f.v;
+  f.c16 = kC16 * f.v;
+  f.c56 = kC56 * f.v;
+  return f;
+}
+
+struct Centre {
+  double s1p, s2p, s3p, s1m, s2m, s3m;
+};
+
+// smoothness terms of centre c from its faces a = c-1, b = c, d = c+1: the
+// three indicators of the plus side (S1+(c-2), S2+(c-1), S3+(c)) and of the
+// minus side (S1-(c+1), S2-(c), S3-(c-1)), each as first term + second term
+// in the reference's order of operations
+template <int EMU>
+__device__ __forceinline__ Centre make_centre(const Face& a, const Face& b, const Face& d) {
+  using Q = Ar<EMU>;
+  const double t2 = Q::s2(b.v, 1), t4 = Q::s2(b.v, 2);
+  double t;
+  t = (d.v - t2) + a.v;
+  const double A = k1312 * (t * t);
+  t = (a.v - t2) + d.v;
+  const double B = k1312 * (t * t);
+  t = (d.v - t4) + a.t3;
+  const double Cp = Q::s2(t * t, -2);
+  t = (d.t3 - t4) + a.v;
+  const double Dp = Q::s2(t * t, -2);
+  t = (a.v - t4) + d.t3;
+  const double Cm = Q::s2(t * t, -2);
+  t = (a.t3 - t4) + d.v;
+  const double Dm = Q::s2(t * t, -2);
+  t = d.v - a.v;
+  const double E = Q::s2(t * t, -2);
+  Centre c;
+  c.s1p = A + Cp;
+  c.s2p = A + E;
+  c.s3p = A + Dp;
+  c.s1m = B + Cm;
+  c.s2m = B + E;
+  c.s3m = B + Dm;
+  return c;
+}
+
+__device__ __forceinline__ double eps_of(double w1, double w2, double w3, double w4, double w5) {
+  using qss_emu::max_nonneg;
+  const double m = max_nonneg(max_nonneg(max_nonneg(max_nonneg(w1, w2), w3), w4), w5);
+  return 1e-6 * m + 1.0e-35;
+}
+
+// weights and combination of one side (3d.f:1999-2014) given the candidate
+// stencils and smoothness indicators
+template <int EMU>
+__device__ __forceinline__ double weno_weights(double p1, double p2, double p3, double S1, double S2, double S3,
+                                               double eps) {
+  using Q = Ar<EMU>;
+  double t, a1, a2, a3;
+  t = S1 + eps;
+  a1 = Q::div(0.1, t * t);
+  t = S2 + eps;
+  a2 = Q::div(0.6, t * t);
+  t = S3 + eps;
+  a3 = Q::div(0.3, t * t);
+  const double inv_sum_a = Q::div(1.0, a1 + a2 + a3);
+  a1 = a1 * inv_sum_a;
+  a2 = a2 * inv_sum_a;
+  a3 = a3 * inv_sum_a;
+  return a1 * p1 + a2 * p2 + a3 * p3;
+}
+
+struct AxisArgs {
+  Box b;
+  const double* phi;
+  double* dplus;
+  double* dminus;
+  double inv;
+  const Ctl* ctl;
+};
+
+// One thread: SEG consecutive voxels along axis AX starting at s0, inside
+// the fill box of that axis.  Faces s0-2 .. s0+SEG+2, centres s0-1 .. s0+SEG.
+template <int AX, int EMU>
+__global__ void __launch_bounds__(128) k_weno_axis(AxisArgs a) {
+  if (a.ctl && !a.ctl->active) return;
+  const Box& b = a.b;
+  // lanes run along i for the y and z passes (coalesced); for the x pass they
+  // run along j and each thread streams its own row through L1
+  int p, q, seg;
+  int lo, hi;
+  if (AX == 0) {
+    p = b.jlo + blockIdx.x * blockDim.x + threadIdx.x;  // j
+    q = b.klo + blockIdx.y;                              // k
+    seg = blockIdx.z;
+    if (p > b.jhi) return;
+    lo = b.ilo;
+    hi = b.ihi;
+  } else {
+    p = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;  // i
+    q = (AX == 1 ? b.klo : b.jlo) + blockIdx.y;          // k for the y pass, j for the z pass
+    seg = blockIdx.z;
+    if (p > b.ihi) return;
+    lo = (AX == 1) ? b.jlo : b.klo;
+    hi = (AX == 1) ? b.jhi : b.khi;
+  }
+  const int s0 = lo + seg * SEG;
+  if (s0 > hi) return;
+  int64_t base, stride;
+  if (AX == 0) {
+    base = b.idx(0, p, q);
+    stride = 1;
+  } else if (AX == 1) {
+    base = b.idx(p, 0, q);
+    stride = b.nx;
+  } else {
+    base = b.idx(p, q, 0);
+    stride = (int64_t)b.nx * b.ny;
+  }
+  const double* __restrict__ phi = a.phi;
+  const double inv = a.inv;
+  // phi along the line, clamped to the last ghost point for the tail segment
+  const int last = (AX == 0 ? b.nx : (AX == 1 ? b.ny : b.nz)) - 1;
+  auto ld = [&](int m) -> double {
+    const int mm = m > last ? last : m;
+    return __ldg(phi + base + (int64_t)mm * stride);
+  };
+
+  // prologue: faces s0-2 .. s0+2, centres s0-1 .. s0+1, eps+(s0-1)
+  double pm3 = ld(s0 - 3), pm2 = ld(s0 - 2), pm1 = ld(s0 - 1), p0 = ld(s0), pp1 = ld(s0 + 1), pp2 = ld(s0 + 2);
+  Face fm2 = make_face(pm2, pm3, inv);  // face s0-2
+  Face fm1 = make_face(pm1, pm2, inv);  // face s0-1
+  Face f0 = make_face(p0, pm1, inv);    // face s0
+  Face f1 = make_face(pp1, p0, inv);    // face s0+1
+  Face f2 = make_face(pp2, pp1, inv);   // face s0+2
+  Centre cm1 = make_centre<EMU>(fm2, fm1, f0);  // centre s0-1
+  Centre c0 = make_centre<EMU>(fm1, f0, f1);    // centre s0
+  Centre c1 = make_centre<EMU>(f0, f1, f2);     // centre s0+1
+  double eps_prev = eps_of(f2.w, f1.w, f0.w, fm1.w, fm2.w);  // eps+(s0-1): faces s0-2 .. s0+2
+  double plast = pp2;
+
+  // fully unrolled, the loop with the integer-pipe arithmetic no longer fits
+  // the instruction cache; the window then rotates by register moves
+#pragma unroll(EMU == 0 ? SEG : 1)
+  for (int t = 0; t < SEG; t++) {
+    const int i = s0 + t;
+    // window: faces i-2 (fm2) .. i+2 (f2); centres i-1 (cm1) .. i+1 (c1)
+    const double pnext = ld(i + 3);
+    const Face f3 = make_face(pnext, plast, inv);  // face i+3
+    const Centre c2 = make_centre<EMU>(f1, f2, f3);     // centre i+2
+    const double eps_i = eps_of(f3.w, f2.w, f1.w, f0.w, fm1.w);  // eps+(i): faces i-1 .. i+3
+    if (i <= hi) {
+      // plus: v1..v5 = faces i+3, i+2, i+1, i, i-1
+      const double pp1_ = (f3.c13 - f2.c76) + f1.c116;
+      const double pp2_ = (-f2.c16 + f1.c56) + f0.c13;
+      const double pp3_ = (f1.c13 + f0.c56) - fm1.c16;
+      const double plus = weno_weights<EMU>(pp1_, pp2_, pp3_, c2.s1p, c1.s2p, c0.s3p, eps_i);
+      // minus: v1..v5 = faces i-2, i-1, i, i+1, i+2
+      const double pm1_ = (fm2.c13 - fm1.c76) + f0.c116;
+      const double pm2_ = (-fm1.c16 + f0.c56) + f1.c13;
+      const double pm3_ = (f0.c13 + f1.c56) - f2.c16;
+      const double minus = weno_weights<EMU>(pm1_, pm2_, pm3_, cm1.s1m, c0.s2m, c1.s3m, eps_prev);
+      const int64_t o = base + (int64_t)i * stride;
+      a.dplus[o] = plus;
+      a.dminus[o] = minus;
+    }
+    // slide the window by one voxel
+    fm2 = fm1;
+    fm1 = f0;
+    f0 = f1;
+    f1 = f2;
+    f2 = f3;
+    cm1 = c0;
+    c0 = c1;
+    c1 = c2;
+    eps_prev = eps_i;
+    plast = pnext;
+  }
+}
+
+struct CombineArgs {
+  Box b;
+  Fac fac;
+  const double* phi_in;
+  const double* u_cur;
+  double* out;
+  double* phi_new;
+  const double* dp[3];
+  const double* dm[3];
+  Coef c;
+  ImposeArgs im;
+  const Ctl* ctl;
+};
+
+// Godunov normal term of the WENO5 scheme, vel * |grad| (3d.f:2245-2276),
+// with the sign tests and maxima on the integer pipes at EMU >= 1
+template <int EMU>
+__device__ __forceinline__ double godunov5(double vel, const double pp[3], const double pm[3]) {
+  if (EMU == 0) return godunov_norm<WENO5>(vel, pp, pm);
+  using namespace qss_emu;
+  double ngps;
+  if (gt0(vel)) {
+    double s[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double a = gt0(pm[d]) ? pm[d] : 0.0, c = lt0(pp[d]) ? pp[d] : 0.0;
+      s[d] = max_nonneg(a * a, c * c);
+    }
+    ngps = s[0] + s[1] + s[2];
+  } else {
+    double s[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double a = lt0(pm[d]) ? pm[d] : 0.0, c = gt0(pp[d]) ? pp[d] : 0.0;
+      s[d] = max_nonneg(a * a, c * c);
+    }
+    ngps = s[0] + s[1] + s[2];
+  }
+  return vel * qss_emu::sqrt(ngps);
+}
+
+// |v| >= 1e-5 (false for NaN)
+__device__ __forceinline__ bool speed_valid(double v) {
+  const uint64_t a = qss_emu::bits(v) & qss_emu::kAbs;
+  return a >= qss_emu::bits(1.e-5) && a <= 0x7ff0000000000000ull;
+}
+
+// central curvature term (3d.f:2336-2378), same operations as curvature()
+// with the exact doublings, the threshold test and the division moved to the
+// integer pipes at EMU >= 1
+template <int EMU>
+__device__ __forceinline__ double curvature_e(const double* __restrict__ phi, const Box& b, int64_t c, const Fac& f) {
+  if (EMU == 0) return curvature(phi, b, c, f);
+  using Q = Ar<EMU>;
+  const int64_t sy = b.sy(), sz = b.sz();
+  const double cc = __ldg(phi + c);
+  const double cc2 = Q::s2(cc, 1);
+  const double phi_x = (__ldg(phi + c + 1) - __ldg(phi + c - 1)) * f.x;
+  const double phi_y = (__ldg(phi + c + sy) - __ldg(phi + c - sy)) * f.y;
+  const double phi_z = (__ldg(phi + c + sz) - __ldg(phi + c - sz)) * f.z;
+  const double phi_xx = (__ldg(phi + c + 2) + __ldg(phi + c - 2) - cc2) * f.x * f.x;
+  const double phi_zz = (__ldg(phi + c + 2 * sz) + __ldg(phi + c - 2 * sz) - cc2) * f.z * f.z;
+  const double phi_yy = (__ldg(phi + c + 2 * sy) + __ldg(phi + c - 2 * sy) - cc2) * f.y * f.y;
+  const double phi_xy = (__ldg(phi + c + 1 + sy) + __ldg(phi + c - 1 - sy) - __ldg(phi + c - 1 + sy) -
+                         __ldg(phi + c + 1 - sy)) * f.x * f.y;
+  const double phi_xz = (__ldg(phi + c + 1 + sz) + __ldg(phi + c - 1 - sz) - __ldg(phi + c - 1 + sz) -
+                         __ldg(phi + c + 1 - sz)) * f.x * f.z;
+  const double phi_yz = (__ldg(phi + c + sy + sz) + __ldg(phi + c - sy - sz) - __ldg(phi + c - sy + sz) -
+                         __ldg(phi + c + sy - sz)) * f.y * f.z;
+  const double grad_mag2 = phi_x * phi_x + phi_y * phi_y + phi_z * phi_z;
+  // grad_mag2 < 1e-5: a sum of squares is +0, positive or NaN
+  if (qss_emu::bits(grad_mag2) < qss_emu::bits(1.e-5)) return 0.0;
+  // at level 2 the products of the curvature numerator run on the integer
+  // pipes (the FP64 pipe is the combine kernel's bound; its integer pipes idle)
+  const double curv = phi_xx * phi_y * phi_y + Q::mul2(Q::mul2(phi_yy, phi_x), phi_x) -
+                      Q::mul2(Q::mul2(Q::s2(phi_xy, 1), phi_x), phi_y) + Q::mul2(Q::mul2(phi_xx, phi_z), phi_z) +
+                      Q::mul2(Q::mul2(phi_zz, phi_x), phi_x) - Q::mul2(Q::mul2(Q::s2(phi_xz, 1), phi_x), phi_z) +
+                      Q::mul2(Q::mul2(phi_yy, phi_z), phi_z) + Q::mul2(Q::mul2(phi_zz, phi_y), phi_y) -
+                      Q::mul2(Q::mul2(Q::s2(phi_yz, 1), phi_y), phi_z);
+  return Q::div(curv, grad_mag2);
+}
+
+// the three mask impositions with the comparisons on the integer pipes
+template <int EMU>
+__device__ __forceinline__ double impose3_e(double v, int64_t idx, const ImposeArgs& im) {
+  if (EMU == 0) return impose3(v, idx, im);
+  double t = im.mask[idx] - im.overlap;
+  v = qss_emu::gt(t, v) ? t : v;
+  if (im.check_conn) {
+    t = im.mask_w[idx] - 0.0;
+    v = qss_emu::gt(t, v) ? t : v;
+    t = im.mask_nw[idx] - 0.0;
+    v = qss_emu::gt(t, v) ? t : v;
+  }
+  return v;
+}
+
+template <int STAGE, bool FINAL, int EMU>
+__global__ void __launch_bounds__(128) k_weno_combine(CombineArgs a) {
+  if (STAGE != 0 && !a.ctl->active) return;
+  using Q = Ar<EMU>;
+  const Box& b = a.b;
+  const int i = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = b.jlo + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = b.klo + blockIdx.z * blockDim.z + threadIdx.z;
+  if (i > b.ihi || j > b.jhi || k > b.khi) return;
+  const int64_t idx = b.idx(i, j, k);
+  double pp[3], pm[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    pp[d] = a.dp[d][idx];
+    pm[d] = a.dm[d][idx];
+  }
+  const double vel = a.c.vel_n[idx];
+  double temp_norm;
+  if (EMU >= 1 ? speed_valid(vel) : fabs(vel) >= 1.e-5) {
+    temp_norm = godunov5<EMU>(vel, pp, pm);
+  } else {
+    const int src = a.c.nsrc[idx];
+    if (src < 0) {
+      temp_norm = 0.0;
+    } else {
+      double qp[3], qm[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        qp[d] = a.dp[d][src];
+        qm[d] = a.dm[d][src];
+      }
+      temp_norm = godunov5<EMU>(a.c.vel_n[src], qp, qm);
+    }
+  }
+  const double vx = a.c.vx[idx], vy = a.c.vy[idx], vz = a.c.vz[idx];
+  double ax, ay, az;
+  if (EMU >= 1) {
+    ax = qss_emu::ge0(vx) ? pm[0] : pp[0];
+    ay = qss_emu::ge0(vy) ? pm[1] : pp[1];
+    az = qss_emu::ge0(vz) ? pm[2] : pp[2];
+  } else {
+    ax = (vx >= 0) ? pm[0] : pp[0];
+    ay = (vy >= 0) ? pm[1] : pp[1];
+    az = (vz >= 0) ? pm[2] : pp[2];
+  }
+  const double temp_vel = -(vx * ax + vy * ay + vz * az);
+  const double temp_curv = a.c.b[idx] * curvature_e<EMU>(a.phi_in, b, idx, a.fac);
+  const double rhs = temp_norm + temp_curv + temp_vel;
+  double out;
+  if (STAGE == 0) {
+    out = rhs;
+  } else {
+    const double dt = a.ctl->dt;
+    const double* __restrict__ phi = a.phi_in;
+    if (STAGE == 1) {
+      out = phi[idx] + dt * rhs;
+    } else if (STAGE == 2) {
+      out = 0.75 * a.u_cur[idx] + Q::s2(phi[idx] + dt * rhs, -2);
+    } else {
+      const double one_third = 1.0 / 3.0, two_thirds = 2.0 / 3.0;
+      out = one_third * a.u_cur[idx] + two_thirds * (phi[idx] + dt * rhs);
+    }
+  }
+  a.out[idx] = out;
+  if (FINAL) a.phi_new[idx] = impose3_e<EMU>(out, idx, a.im);
+}
+
+template <int EMU>
+void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[3], double* const dp[3],
+             double* const dm[3], const Ctl* ctl) {
+  for (int ax = 0; ax < 3; ax++) {
+    AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl};
+    const int along = ax == 0 ? b.fbx() : (ax == 1 ? b.fby() : b.fbz());
+    const int lanes = ax == 0 ? b.fby() : b.fbx();
+    const int other = ax == 2 ? b.fby() : b.fbz();
+    dim3 g((lanes + 127) / 128, other, (along + SEG - 1) / SEG);
+    cudaEvent_t e0 = ctl ? prof_open(s) : nullptr;
+    if (ax == 0) k_weno_axis<0, EMU><<<g, 128, 0, s>>>(a);
+    else if (ax == 1) k_weno_axis<1, EMU><<<g, 128, 0, s>>>(a);
+    else k_weno_axis<2, EMU><<<g, 128, 0, s>>>(a);
+    prof_close(s, e0, kProfAxisX + ax);
+  }
+}
+
+template <int EMU>
+void combine_at(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
+  switch (stage) {
+    case 0: k_weno_combine<0, false, EMU><<<g, blk, 0, s>>>(a); break;
+    case 1: if (final_stage) k_weno_combine<1, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU><<<g, blk, 0, s>>>(a); break;
+    case 2: if (final_stage) k_weno_combine<2, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU><<<g, blk, 0, s>>>(a); break;
+    default: if (final_stage) k_weno_combine<3, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU><<<g, blk, 0, s>>>(a); break;
+  }
+}
+
+}  // namespace
+
+void launch_weno_axes(cudaStream_t s, const Box& b, const double* phi, double dx, double dy, double dz,
+                      double* const dp[3], double* const dm[3], const Ctl* ctl) {
+  const double invs[3] = {1.0 / dx, 1.0 / dy, 1.0 / dz};
+  if (emu_level() == 0) axes_at<0>(s, b, phi, invs, dp, dm, ctl);
+  else axes_at<1>(s, b, phi, invs, dp, dm, ctl);
+}
+
+void launch_weno_combine(cudaStream_t s, int stage, bool final_stage, const Box& b, double dx, double dy, double dz,
+                         const double* phi_in, const double* u_cur, double* out, double* phi_new,
+                         double* const dp[3], double* const dm[3], const Coef& c, const ImposeArgs& im,
+                         const Ctl* ctl) {
+  CombineArgs a;
+  a.b = b;
+  a.fac = Fac{0.5 / dx, 0.5 / dy, 0.5 / dz};
+  a.phi_in = phi_in;
+  a.u_cur = u_cur;
+  a.out = out;
+  a.phi_new = phi_new;
+  for (int d = 0; d < 3; d++) {
+    a.dp[d] = dp[d];
+    a.dm[d] = dm[d];
+  }
+  a.c = c;
+  a.im = im;
+  a.ctl = ctl;
+  const dim3 blk(32, 4, 1);
+  const dim3 g((b.fbx() + 31) / 32, (b.fby() + 3) / 4, b.fbz());
+  cudaEvent_t e0 = stage != 0 ? prof_open(s) : nullptr;
+  switch (emu_level()) {
+    case 0: combine_at<0>(s, stage, final_stage, g, blk, a); break;
+    case 1: combine_at<1>(s, stage, final_stage, g, blk, a); break;
+    default: combine_at<2>(s, stage, final_stage, g, blk, a); break;
+  }
+  prof_close(s, e0, kProfCombine);
+}
+
+}  // namespace qss

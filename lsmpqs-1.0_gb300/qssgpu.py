@@ -161,6 +161,10 @@ def load(path: str) -> C.CDLL:
         "qssgpu_clear_error": (None, []),
         "qssgpu_device_available": (C.c_int, []),
         "qssgpu_set_slabs": (None, [C.c_int]),
+        "qssgpu_set_weno_split": (C.c_int, [C.c_int]),
+        "qssgpu_set_emu_level": (C.c_int, [C.c_int]),
+        "qssgpu_emu_selftest": (C.c_int, [C.c_longlong, C.c_ulonglong, P(C.c_longlong), P(C.c_double)]),
+        "qssgpu_op_rates": (C.c_int, [P(C.c_double)]),
         "qssgpu_get_slabs": (C.c_int, [C.c_void_p]),
         "qssgpu_release": (None, [P(QSSDataArrays)]),
         "qssgpu_call_stats": (None, [P(QSSDataArrays), P(Grid), P(C.c_longlong), P(C.c_longlong)]),

@@ -73,6 +73,41 @@ def test_rhs_slab_and_tiny_speed(gpu, oracle, name, var):
         assert a[1] == o[1]
 
 
+@pytest.mark.parametrize("split,emu", [(0, 2), (1, 0), (1, 1), (1, 2)])
+@pytest.mark.parametrize("small", [0.0, 0.2])
+def test_weno5_split_and_fused(gpu, oracle, split, emu, small):
+    """The WENO5 stage runs either as three axis passes with shared
+    sub-expressions + a combine kernel (with 0, 1 or 2 levels of FP64
+    arithmetic on the integer pipes), or as one fused kernel; all equal the
+    oracle bit for bit, on the whole fill box and on a z-slab."""
+    g, _ = pack_case(oracle, N)
+    phi, vel, b, vx, vy, vz = _fields(g, 5, small)
+    prev = gpu.qssgpu_set_weno_split(split)
+    prev_emu = gpu.qssgpu_set_emu_level(emu)
+    try:
+        for klo, khi in ((None, None), (g.klo_fb + 3, g.klo_fb + 9)):
+            a = _run_rhs(gpu, "getrhs3d5th_", True, g, phi, vel, b, vx, vy, vz, klo, khi)
+            o = _run_rhs(oracle, "getrhs3d5th_", True, g, phi, vel, b, vx, vy, vz, klo, khi)
+            Q.check(gpu)
+            assert np.array_equal(a[0], o[0]), f"max |d| = {np.abs(a[0] - o[0]).max()}"
+            assert a[1] == o[1]
+    finally:
+        gpu.qssgpu_set_weno_split(prev)
+        gpu.qssgpu_set_emu_level(prev_emu)
+
+
+def test_emu_selftest(gpu):
+    """Integer-pipe FP64 division, square root, product, sum, difference,
+    power-of-two scaling, comparisons and maxima equal the native instructions on 2^24
+    generated operand pairs (all classes of doubles)."""
+    counts = (C.c_longlong * 9)()
+    first = (C.c_double * 3)()
+    assert gpu.qssgpu_emu_selftest(1 << 24, 20261203, counts, first) == 0
+    Q.check(gpu)
+    assert counts[8] == 1 << 24
+    assert list(counts[:8]) == [0] * 8, f"mismatch: op {first[0]} x={first[1]!r} y={first[2]!r}"
+
+
 def test_rk_stages(gpu, oracle):
     g, _ = pack_case(oracle, N)
     rng = np.random.default_rng(3)

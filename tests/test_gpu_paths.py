@@ -105,6 +105,30 @@ def test_const_curv_model(gpu, oracle, theta, space, time):
     assert diff_arrays(vg, vo) == {}
 
 
+@pytest.mark.parametrize("split,emu", [(0, 2), (1, 0), (1, 1), (1, 2)])
+def test_const_curv_model_weno_modes(gpu, oracle, split, emu):
+    """WENO5 + TVD-RK3 with variable coefficients through the fused stage
+    kernel and through the axis passes + combine: both equal the oracle."""
+    g, v = pack_case(oracle, 22, seed=4)
+    o_g = options(gpu, 40, 5, 3, tmax=0.02, tplot=0.01)
+    o_o = options(oracle, 40, 5, 3, tmax=0.02, tplot=0.01)
+    vg, vo = clone(v), clone(v)
+    prepare_model(oracle, o_g, vg, 1.25)
+    prepare_model(oracle, o_o, vo, 1.25)
+    gpu.setSpaceDerivFunc(C.byref(g), C.byref(o_g))
+    prev = gpu.qssgpu_set_weno_split(split)
+    prev_emu = gpu.qssgpu_set_emu_level(emu)
+    try:
+        tg = _model(gpu, vg, o_g, True, 1.25)
+    finally:
+        gpu.qssgpu_set_weno_split(prev)
+        gpu.qssgpu_set_emu_level(prev_emu)
+    to = _model(oracle, vo, o_o, True, 1.25)
+    Q.check(gpu)
+    assert tg == to
+    assert diff_arrays(vg, vo) == {}
+
+
 @pytest.mark.parametrize("slabs", [2, 5])
 def test_const_curv_model_slabs(gpu, oracle, slabs):
     """The reference's dt uses the last voxel of each OpenMP z-slab; with
