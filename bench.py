@@ -179,6 +179,7 @@ KERNEL_NAME = {0: "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
                2: "k_weno_axis<1> (WENO5 y-pass, shared sub-expressions)",
                3: "k_weno_axis<2> (WENO5 z-pass, shared sub-expressions)",
                4: "k_weno_combine (Godunov + advection + curvature + TVD-RK)"}
+N_KINDS = 5
 # algorithmic HBM bytes per voxel-step (each array touched once per stage):
 # stage 1 phi + 5 coefficients -> phi1, stage 2 phi1 + phi + 5 coeff -> phi2,
 # stage 3 phi2 + phi + 5 coeff + 3 masks -> phi1, phi
@@ -201,7 +202,7 @@ def gpu_arm(args, dist: Dist):
     if lib.qssgpu_prepare_step(C.byref(o), C.byref(v.p), C.byref(g), a0):
         Q.check(lib)
     nvox = n ** 3
-    out = (C.c_double * 15)()
+    out = (C.c_double * (5 + 2 * N_KINDS))()
     dist.barrier()
     with ClockSampler(dist.local) as clk:
         lib.qssgpu_time_steps(C.byref(o), C.byref(v.p), C.byref(g), a0, args.warmup, args.steps, out)
@@ -211,9 +212,10 @@ def gpu_arm(args, dist: Dist):
     value = dist.ws * nvox * args.steps / (ms / 1e3)
     top = int(out[4])
     top_ms = out[1]
-    kinds = {KERNEL_NAME[k].split(" ")[0]: {"ms_total": round(out[5 + k], 3), "launches": int(out[10 + k]),
+    kinds = {KERNEL_NAME[k].split(" ")[0]: {"ms_total": round(out[5 + k], 3),
+                                            "launches": int(out[5 + N_KINDS + k]),
                                             "share_of_step": round(out[5 + k] / ms, 4) if ms else None}
-             for k in range(5) if out[10 + k] > 0}
+             for k in range(N_KINDS) if out[5 + N_KINDS + k] > 0}
     launches = int(out[2]) * args.steps
 
     # e2e through the C entry point with host arrays: one outer iteration of

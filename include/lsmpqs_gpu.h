@@ -206,10 +206,10 @@ int qssgpu_device_available(void);
    count of the reference run to reproduce (default 1, or $QSSGPU_SLABS);
    0 restores the default */
 void qssgpu_set_slabs(int nslabs);
-/* WENO5 variable-coefficient stages as three axis passes + a combine kernel
-   (1, the default) or as one fused kernel per stage (0; also
-   $QSSGPU_WENO_FUSED=1); -1 restores the default; results are identical.
-   Returns the previous mode. */
+/* WENO5 variable-coefficient stages: 0 one fused kernel per stage, 1 (the
+   default) one kernel per axis + a combine kernel; also $QSSGPU_WENO_MODE;
+   -1 restores the default; results are identical.  Returns the previous
+   mode. */
 int qssgpu_set_weno_split(int mode);
 /* Share of the split WENO5 stage's FP64 arithmetic computed bit-exactly on
    the integer pipes: 0 none, 1 divisions, power-of-two scalings and

@@ -159,7 +159,8 @@ double dev_maxnorm(DevVolume& v, const Options* o) {
 void enqueue_stage(DevVolume& v, const SchemeSel& sc, const Coef& c, const ImposeArgs& im, int stage, bool fin,
                    const double* in, double* out, double* phi_new, const Grid* g) {
   const double dx = g->dx[0], dy = g->dx[1], dz = g->dx[2];
-  if (sc.scheme == WENO5 && sc.var && weno_split()) {
+  const int mode = (sc.scheme == WENO5 && sc.var) ? weno_mode() : 0;
+  if (mode == 1) {
     launch_weno_axes(v.stream, v.box, in, dx, dy, dz, v.dplus, v.dminus, v.ctl);
     launch_weno_combine(v.stream, stage, fin, v.box, dx, dy, dz, in, v.phi, out, phi_new, v.dplus, v.dminus, c,
                         im, v.ctl);
@@ -197,8 +198,8 @@ void enqueue_step(DevVolume& v, const SchemeSel& sc, const Coef& c, const Impose
   }
 }
 
-int kernels_per_step(int order, bool split) {
-  const int per_stage = split ? 4 : 1;
+int kernels_per_step(int order, int mode) {
+  const int per_stage = mode == 1 ? 4 : 1;
   const int stages = order <= 1 ? 1 : (order == 2 ? 2 : 3);
   return 1 + stages * (per_stage + 1) + (order <= 1 ? 1 : 0);
 }
@@ -370,7 +371,7 @@ double path_inner_loop(DevVolume& v, Options* o, Grid* g, double a, int max_step
 }
 int path_kernels_per_step(DevVolume& v, const Options* o) {
   SchemeSel sc = scheme_of(o);
-  return kernels_per_step(o->order_time_accur, sc.scheme == WENO5 && sc.var && weno_split());
+  return kernels_per_step(o->order_time_accur, (sc.scheme == WENO5 && sc.var) ? weno_mode() : 0);
 }
 void path_upload_for_const_curv(DevVolume& v, QSS_DataArrays* p, const Options* o, bool var) {
   upload_for_const_curv(v, p, o, var);

@@ -126,7 +126,8 @@ void rhs_entry(int scheme, bool var, const double* phi, const double* vel_n, con
     c.b_const = *b;
   }
   ImposeArgs im{};
-  if (scheme == WENO5 && var && weno_split()) {
+  const int mode = (scheme == WENO5 && var) ? weno_mode() : 0;
+  if (mode != 0) {
     DBuf d0(bytes), d1(bytes), d2(bytes), d3(bytes), d4(bytes), d5(bytes);
     double* const dp[3] = {d0.d(), d1.d(), d2.d()};
     double* const dm[3] = {d3.d(), d4.d(), d5.d()};

@@ -466,7 +466,7 @@ int qssgpu_time_steps(Options* o, QSS_DataArrays* p, Grid* g, double a0, int war
   out[4] = top;
   for (int k = 0; k < kProfKinds; k++) {
     out[5 + k] = kind_ms[k];
-    out[10 + k] = kind_n[k];
+    out[5 + kProfKinds + k] = kind_n[k];
   }
   return 0;
   QSS_API_END(return 1)

@@ -85,13 +85,13 @@ int num_slabs_for(const Grid* g) {
   return t;
 }
 
-bool weno_split() {
+int weno_mode() {
   int m = g_weno_split;
   if (m < 0) {
-    const char* e = getenv("QSSGPU_WENO_FUSED");
-    m = (e && atoi(e) == 1) ? 0 : 1;
+    const char* e = getenv("QSSGPU_WENO_MODE");
+    m = e ? atoi(e) : 1;
   }
-  return m != 0;
+  return m <= 0 ? 0 : 1;
 }
 
 int emu_level() {
@@ -318,7 +318,7 @@ int qssgpu_set_emu_level(int level) {
 }
 
 int qssgpu_set_weno_split(int mode) {
-  const int prev = weno_split() ? 1 : 0;
+  const int prev = weno_mode();
   g_weno_split = mode < 0 ? -1 : (mode ? 1 : 0);
   return prev;
 }

@@ -95,10 +95,10 @@ void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which);
 void download_dirty(DevVolume& v, QSS_DataArrays* p);
 
 int num_slabs_for(const Grid* g);
-// WENO5 variable-coefficient stages as axis passes + combine (true, default)
-// or as the single fused stage kernel ($QSSGPU_WENO_FUSED=1,
-// qssgpu_set_weno_split(0)); both give identical results
-bool weno_split();
+// WENO5 variable-coefficient stages: 0 one fused kernel per stage, 1 (default)
+// one kernel per axis + a combine kernel ($QSSGPU_WENO_MODE,
+// qssgpu_set_weno_split); both give identical results
+int weno_mode();
 // share of the WENO5 stage's FP64 arithmetic done on the integer pipes
 // (0 none, 1 divisions / power-of-two scalings / comparisons, 2 also part of
 // the products and sums; $QSSGPU_EMU, qssgpu_set_emu_level); all levels give

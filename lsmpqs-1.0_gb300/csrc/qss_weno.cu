@@ -44,11 +44,12 @@ constexpr int SEG = 16;  // voxels per thread along the pass axis
 //   0: native FP64 instructions only;
 //   1: divisions, square roots, power-of-two scalings and comparisons on the
 //      integer pipes;
-//   2: level 1 plus the products of the curvature numerator in the combine
-//      kernel, which runs with enough warps per scheduler to overlap them with
-//      its FP64 work.  (The axis passes hold ~120 registers per thread, too
-//      few warps to hide the latency of more integer-pipe arithmetic; they run
-//      at level 1 for levels 1 and 2.)
+//   2: level 1 plus a share of the products: in the axis passes the five
+//      scaled copies of each face and the normalised weights, in the combine
+//      kernel the second derivatives and the curvature numerator.  The
+//      combine kernel runs ~10 warps per scheduler and overlaps these with
+//      its FP64 work; the axis passes hold ~120 registers per thread (4 warps
+//      per scheduler) and gain only a few percent from them.
 template <int EMU>
 struct Ar {
   static __device__ __forceinline__ double div(double a, double b) {
@@ -82,6 +83,24 @@ __device__ __forceinline__ Face make_face(double hi, double lo, double inv) {
   f.c116 = kC116 * f.v;
   f.c16 = kC16 * f.v;
   f.c56 = kC56 * f.v;
+  return f;
+}
+
+// the same face with its five scaled copies on the integer pipes at EMU >= 2
+template <int EMU>
+__device__ __forceinline__ Face make_face_e(double hi, double lo, double inv) {
+  if (EMU < 2) return make_face(hi, lo, inv);
+  using qss_emu::mul;
+  Face f;
+  const double d = hi - lo;
+  f.v = d * inv;
+  f.w = f.v * f.v;
+  f.t3 = 3.0 * f.v;
+  f.c13 = mul(kC13, f.v);
+  f.c76 = mul(kC76, f.v);
+  f.c116 = mul(kC116, f.v);
+  f.c16 = mul(kC16, f.v);
+  f.c56 = mul(kC56, f.v);
   return f;
 }
 
@@ -142,9 +161,9 @@ __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, 
   t = S3 + eps;
   a3 = Q::div(0.3, t * t);
   const double inv_sum_a = Q::div(1.0, a1 + a2 + a3);
-  a1 = a1 * inv_sum_a;
-  a2 = a2 * inv_sum_a;
-  a3 = a3 * inv_sum_a;
+  a1 = Q::mul2(a1, inv_sum_a);
+  a2 = Q::mul2(a2, inv_sum_a);
+  a3 = Q::mul2(a3, inv_sum_a);
   return a1 * p1 + a2 * p2 + a3 * p3;
 }
 
@@ -206,11 +225,11 @@ __global__ void __launch_bounds__(128) k_weno_axis(AxisArgs a) {
 
   // prologue: faces s0-2 .. s0+2, centres s0-1 .. s0+1, eps+(s0-1)
   double pm3 = ld(s0 - 3), pm2 = ld(s0 - 2), pm1 = ld(s0 - 1), p0 = ld(s0), pp1 = ld(s0 + 1), pp2 = ld(s0 + 2);
-  Face fm2 = make_face(pm2, pm3, inv);  // face s0-2
-  Face fm1 = make_face(pm1, pm2, inv);  // face s0-1
-  Face f0 = make_face(p0, pm1, inv);    // face s0
-  Face f1 = make_face(pp1, p0, inv);    // face s0+1
-  Face f2 = make_face(pp2, pp1, inv);   // face s0+2
+  Face fm2 = make_face_e<EMU>(pm2, pm3, inv);  // face s0-2
+  Face fm1 = make_face_e<EMU>(pm1, pm2, inv);  // face s0-1
+  Face f0 = make_face_e<EMU>(p0, pm1, inv);    // face s0
+  Face f1 = make_face_e<EMU>(pp1, p0, inv);    // face s0+1
+  Face f2 = make_face_e<EMU>(pp2, pp1, inv);   // face s0+2
   Centre cm1 = make_centre<EMU>(fm2, fm1, f0);  // centre s0-1
   Centre c0 = make_centre<EMU>(fm1, f0, f1);    // centre s0
   Centre c1 = make_centre<EMU>(f0, f1, f2);     // centre s0+1
@@ -224,7 +243,7 @@ __global__ void __launch_bounds__(128) k_weno_axis(AxisArgs a) {
     const int i = s0 + t;
     // window: faces i-2 (fm2) .. i+2 (f2); centres i-1 (cm1) .. i+1 (c1)
     const double pnext = ld(i + 3);
-    const Face f3 = make_face(pnext, plast, inv);  // face i+3
+    const Face f3 = make_face_e<EMU>(pnext, plast, inv);  // face i+3
     const Centre c2 = make_centre<EMU>(f1, f2, f3);     // centre i+2
     const double eps_i = eps_of(f3.w, f2.w, f1.w, f0.w, fm1.w);  // eps+(i): faces i-1 .. i+3
     if (i <= hi) {
@@ -316,16 +335,16 @@ __device__ __forceinline__ double curvature_e(const double* __restrict__ phi, co
   const double phi_x = (__ldg(phi + c + 1) - __ldg(phi + c - 1)) * f.x;
   const double phi_y = (__ldg(phi + c + sy) - __ldg(phi + c - sy)) * f.y;
   const double phi_z = (__ldg(phi + c + sz) - __ldg(phi + c - sz)) * f.z;
-  const double phi_xx = (__ldg(phi + c + 2) + __ldg(phi + c - 2) - cc2) * f.x * f.x;
-  const double phi_zz = (__ldg(phi + c + 2 * sz) + __ldg(phi + c - 2 * sz) - cc2) * f.z * f.z;
-  const double phi_yy = (__ldg(phi + c + 2 * sy) + __ldg(phi + c - 2 * sy) - cc2) * f.y * f.y;
-  const double phi_xy = (__ldg(phi + c + 1 + sy) + __ldg(phi + c - 1 - sy) - __ldg(phi + c - 1 + sy) -
-                         __ldg(phi + c + 1 - sy)) * f.x * f.y;
-  const double phi_xz = (__ldg(phi + c + 1 + sz) + __ldg(phi + c - 1 - sz) - __ldg(phi + c - 1 + sz) -
-                         __ldg(phi + c + 1 - sz)) * f.x * f.z;
-  const double phi_yz = (__ldg(phi + c + sy + sz) + __ldg(phi + c - sy - sz) - __ldg(phi + c - sy + sz) -
-                         __ldg(phi + c + sy - sz)) * f.y * f.z;
-  const double grad_mag2 = phi_x * phi_x + phi_y * phi_y + phi_z * phi_z;
+  const double phi_xx = Q::mul2((__ldg(phi + c + 2) + __ldg(phi + c - 2) - cc2) * f.x, f.x);
+  const double phi_zz = Q::mul2((__ldg(phi + c + 2 * sz) + __ldg(phi + c - 2 * sz) - cc2) * f.z, f.z);
+  const double phi_yy = Q::mul2((__ldg(phi + c + 2 * sy) + __ldg(phi + c - 2 * sy) - cc2) * f.y, f.y);
+  const double phi_xy = Q::mul2((__ldg(phi + c + 1 + sy) + __ldg(phi + c - 1 - sy) - __ldg(phi + c - 1 + sy) -
+                                 __ldg(phi + c + 1 - sy)) * f.x, f.y);
+  const double phi_xz = Q::mul2((__ldg(phi + c + 1 + sz) + __ldg(phi + c - 1 - sz) - __ldg(phi + c - 1 + sz) -
+                                 __ldg(phi + c + 1 - sz)) * f.x, f.z);
+  const double phi_yz = Q::mul2((__ldg(phi + c + sy + sz) + __ldg(phi + c - sy - sz) - __ldg(phi + c - sy + sz) -
+                                 __ldg(phi + c + sy - sz)) * f.y, f.z);
+  const double grad_mag2 = Q::mul2(phi_x, phi_x) + Q::mul2(phi_y, phi_y) + Q::mul2(phi_z, phi_z);
   // grad_mag2 < 1e-5: a sum of squares is +0, positive or NaN
   if (qss_emu::bits(grad_mag2) < qss_emu::bits(1.e-5)) return 0.0;
   // at level 2 the products of the curvature numerator run on the integer
@@ -452,8 +471,10 @@ void combine_at(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, c
 void launch_weno_axes(cudaStream_t s, const Box& b, const double* phi, double dx, double dy, double dz,
                       double* const dp[3], double* const dm[3], const Ctl* ctl) {
   const double invs[3] = {1.0 / dx, 1.0 / dy, 1.0 / dz};
-  if (emu_level() == 0) axes_at<0>(s, b, phi, invs, dp, dm, ctl);
-  else axes_at<1>(s, b, phi, invs, dp, dm, ctl);
+  const int lv = emu_level();
+  if (lv == 0) axes_at<0>(s, b, phi, invs, dp, dm, ctl);
+  else if (lv == 1) axes_at<1>(s, b, phi, invs, dp, dm, ctl);
+  else axes_at<2>(s, b, phi, invs, dp, dm, ctl);
 }
 
 void launch_weno_combine(cudaStream_t s, int stage, bool final_stage, const Box& b, double dx, double dy, double dz,

@@ -76,9 +76,9 @@ def test_rhs_slab_and_tiny_speed(gpu, oracle, name, var):
 @pytest.mark.parametrize("split,emu", [(0, 2), (1, 0), (1, 1), (1, 2)])
 @pytest.mark.parametrize("small", [0.0, 0.2])
 def test_weno5_split_and_fused(gpu, oracle, split, emu, small):
-    """The WENO5 stage runs either as three axis passes with shared
-    sub-expressions + a combine kernel (with 0, 1 or 2 levels of FP64
-    arithmetic on the integer pipes), or as one fused kernel; all equal the
+    """The WENO5 stage runs as one fused kernel (split 0) or as one kernel per
+    axis with shared sub-expressions + a combine kernel (split 1), with 0, 1
+    or 2 levels of FP64 arithmetic on the integer pipes; all equal the
     oracle bit for bit, on the whole fill box and on a z-slab."""
     g, _ = pack_case(oracle, N)
     phi, vel, b, vx, vy, vz = _fields(g, 5, small)
