@@ -302,6 +302,103 @@ def _fill_host_coefficients(lib, o, w, a0):
     Q.check(lib)
 
 
+def batched_arm(args):
+    """Batched mode on uneven volumes: sides uniform in 48..160 voxels (seed 2),
+    porosity uniform in 0.30..0.40, contact angle uniform in 0..60 degrees and
+    a curvature ladder per volume, WENO5 + TVD-RK3.  The same volumes run once
+    through the plain single-volume path (drain_model3d per volume, one after
+    the other) and once through qssgpu_ladder_batch; every volume must end
+    bit-identical.  Returns voxel-steps/s of both (wall clock, host arrays,
+    uploads and downloads included)."""
+    lib = Q.load(Q.GPU_LIB)
+    rng = np.random.default_rng(2)
+    nv = args.batch_volumes
+    sides = rng.integers(48, 161, nv)
+    poros = rng.uniform(0.30, 0.40, nv)
+    thetas = rng.uniform(0.0, 60.0, nv)
+    a0s = rng.uniform(1.0, 1.5, nv)
+    vols = []
+    for i in range(nv):
+        n = int(sides[i])
+        g = Q.make_grid(lib, n)
+        v = Q.Volume(g)
+        m = S.lognormal(n, mu=math.log(6.0), sigma=0.3, porosity=float(poros[i]), seed=100 + i).mask()
+        v["mask"][...] = m
+        v["phi"][...] = S.initial_phi(m, n)
+        o = Q.default_options(lib)
+        o.theta = float(thetas[i]) * 3.14159 / 180
+        o.order_space_accur, o.order_time_accur = 5, 3
+        o.a, o.b, o.dc = float(a0s[i]), 0.04, 0.9722
+        o.amax = o.a + (args.batch_steps - 0.5) * o.b * o.dc
+        o.tmax, o.tplot = 0.05, 0.02
+        o.check_connectivity = 1
+        vols.append((n, g, v, o))
+
+    def copy_opts(o):
+        c = Q.Options()
+        C.pointer(c)[0] = o
+        return c
+
+    def clone(v):
+        w = Q.Volume(v.g)
+        w.copy_from(v)
+        return w
+
+    # plain path: one volume at a time (the drain_model3d ladder without its
+    # per-step files, as in the batched run)
+    plain, stats, phases_plain = [], [], []
+    t0 = time.perf_counter()
+    for n, g, v, o in vols:
+        w, oo = clone(v), copy_opts(o)
+        one_o = (C.POINTER(Q.Options) * 1)(C.pointer(oo))
+        one_p = (C.POINTER(Q.QSSDataArrays) * 1)(C.pointer(w.p))
+        one_g = (C.POINTER(Q.Grid) * 1)(C.pointer(g))
+        if lib.qssgpu_ladder_batch(1, 1, one_o, one_p, one_g, None, None, 1):
+            Q.check(lib)
+        s_in, s_out = C.c_longlong(0), C.c_longlong(0)
+        lib.qssgpu_call_stats(C.byref(w.p), C.byref(g), C.byref(s_in), C.byref(s_out))
+        stats.append(s_in.value)
+        ph = (C.c_double * 8)()
+        lib.qssgpu_call_times(C.byref(w.p), C.byref(g), ph)
+        phases_plain.append(list(ph))
+        lib.qssgpu_release(C.byref(w.p))
+        plain.append(w)
+    t_plain = time.perf_counter() - t0
+    # batched
+    batch = [clone(v) for _, _, v, _ in vols]
+    opts_b = [copy_opts(o) for *_, o in vols]
+    arr_o = (C.POINTER(Q.Options) * nv)(*[C.pointer(o) for o in opts_b])
+    arr_p = (C.POINTER(Q.QSSDataArrays) * nv)(*[C.pointer(b.p) for b in batch])
+    arr_g = (C.POINTER(Q.Grid) * nv)(*[C.pointer(g) for _, g, _, _ in vols])
+    t0 = time.perf_counter()
+    rc = lib.qssgpu_ladder_batch(1, nv, arr_o, arr_p, arr_g, None, None, args.batch_workers)
+    t_batch = time.perf_counter() - t0
+    if rc:
+        raise RuntimeError(f"batched mode: {rc} volumes failed: {lib.qssgpu_error_string().decode()}")
+    exact = all(np.array_equal(batch[i].arrays[k], plain[i].arrays[k]) for i in range(nv)
+                for k in batch[i].arrays)
+    phases_batch = []
+    for b, (_, g, _, _) in zip(batch, vols):
+        ph = (C.c_double * 8)()
+        lib.qssgpu_call_times(C.byref(b.p), C.byref(g), ph)
+        phases_batch.append(list(ph))
+        lib.qssgpu_release(C.byref(b.p))
+    names = ["total", "setup", "upload", "inner", "trap", "reinit", "reduce", "download"]
+    sum_plain = {k: round(sum(p[i] for p in phases_plain), 3) for i, k in enumerate(names)}
+    sum_batch = {k: round(sum(p[i] for p in phases_batch), 3) for i, k in enumerate(names)}
+    work = sum(float(n) ** 3 * st for (n, *_), st in zip(vols, stats))
+    return {"volumes": nv, "sides": [int(x) for x in (sides.min(), sides.max())],
+            "fill_voxels": int(sum(int(x) ** 3 for x in sides)), "ladder_steps": args.batch_steps,
+            "inner_steps_total": int(sum(stats)), "workers": args.batch_workers or nv,
+            "plain": {"value": work / t_plain, "wall_s": t_plain},
+            "batched": {"value": work / t_batch, "wall_s": t_batch},
+            "speedup": t_plain / t_batch, "per_volume_exact": bool(exact), "unit": UNIT,
+            "phase_seconds_summed_over_volumes": {"plain": sum_plain, "batched": sum_batch},
+            "note": "wall clock of drain_model3d ladders with host arrays (WENO5 + TVD-RK3, tplot 0.02, "
+                    "tmax 0.05, reinit and trapping included, no per-step files); plain = one volume "
+                    "after the other, batched = all volumes in one qssgpu_ladder_batch call"}
+
+
 def cpu_arm(args, nz: int, steps: int, warmup: int, threads: int):
     """The reference algorithm on the host cores (CPU oracle, OpenMP) on a
     512 x 512 x nz slab of the workload; returns voxel-steps/s and details."""
@@ -340,6 +437,11 @@ def main():
     ap.add_argument("--cpu-nz", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--fp64-peak", type=float, default=1.25)
+    ap.add_argument("--batched", action="store_true", help="also measure batched mode (uneven volumes)")
+    ap.add_argument("--batch-volumes", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-workers", type=int, default=0)
+    ap.add_argument("--batch-only", action="store_true", help="measure batched mode only")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per stage launch from an ncu capture (optional)")
     args = ap.parse_args()
@@ -368,6 +470,11 @@ def main():
         dist.close()
         return
 
+    if args.batch_only:
+        if dist.rank == 0:
+            print(json.dumps({"batched_mode": batched_arm(args)}))
+        dist.close()
+        return
     res = gpu_arm(args, dist)
     cpu = None
     if dist.rank == 0 and args.cpu:
@@ -383,6 +490,8 @@ def main():
                            "l2": "inputs larger than L2 (each FP64 array 1.1 GB)"},
                 "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "roofline": res["roofline"],
                 "cpu_baseline": cpu, "clocks": res["clocks"]}
+        if args.batched:
+            line["batched_mode"] = batched_arm(args)
         print(json.dumps(line))
     dist.close()
 

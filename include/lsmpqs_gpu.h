@@ -217,6 +217,24 @@ int qssgpu_set_weno_split(int mode);
    products and sums; -1 restores the default.  Results are identical at
    every level.  Returns the previous level. */
 int qssgpu_set_emu_level(int level);
+/* Batched mode (no reference counterpart): the curvature ladder of
+   drain_model3d (drain != 0) or imbibe_model3d on n independent volumes at
+   once, each with its own Options (contact angle, curvature ladder), arrays
+   and grid, on its own CUDA stream driven by one of `workers` host threads
+   (0: one per volume; at most 64).  Every volume ends exactly as a single
+   drain_model3d / imbibe_model3d call on it would leave it.  fp may be NULL
+   or hold n FILE* (each may be NULL).  The per-step files of volume v are
+   named prefix[v] + "data_step_<k>" ("" gives the reference's names); a
+   NULL prefix array or entry writes no per-step files.  Volumes must not
+   share arrays or options.  Returns 0, or the number of volumes that
+   failed; qssgpu_last_error / qssgpu_error_string then describe the first. */
+int qssgpu_ladder_batch(int drain, int n, Options *const *o, QSS_DataArrays *const *p, Grid *const *g,
+                        FILE *const *fp, const char *const *prefix, int workers);
+/* The sequentially rounded sum values[0] + values[1] + ... + values[n-1]
+   (a plain C loop's result, bit for bit) computed on the GPU: in parallel
+   by binade-wise integer sums for non-negative runs, element by element
+   elsewhere; the volume integrals use the same code.  0 on success. */
+int qssgpu_loop_sum(const double *values, long long n, double *out);
 /* Device self-test of the integer-pipe FP64 arithmetic against the native
    instructions on n generated operand pairs: counts[0..7] = mismatches of
    div, mul, add, sub, scale2, comparisons, max, sqrt; counts[8] = cases run
@@ -234,6 +252,13 @@ void qssgpu_release(QSS_DataArrays *p);
 /* inner steps and outer iterations of the last top-level call on p */
 void qssgpu_call_stats(const QSS_DataArrays *p, const Grid *g, long long *inner_steps,
                        long long *outer_iters);
+/* host wall time (s) of the last top-level call on p by phase: out[0] total,
+   out[1] set-up (device arrays), out[2] uploads, out[3] inner steps,
+   out[4] trapping, out[5] reinitialisation, out[6] volume and max-norm
+   reductions, out[7] downloads (out holds 8 doubles); device work is
+   charged to the phase that waits for it, unless $QSSGPU_PHASE_SYNC=1 ends
+   every phase with a stream synchronisation */
+void qssgpu_call_times(const QSS_DataArrays *p, const Grid *g, double *out);
 /* benchmark support: drain_model3d's set-up for curvature a0 with the arrays
    left in HBM, then timing of `steps` inner steps after `warmup`
    (out[0] total ms, out[1] mean ms per launch of the stage kernel with the

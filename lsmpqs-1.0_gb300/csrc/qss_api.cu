@@ -100,6 +100,7 @@ int reinit_iterations(const Grid* g, const Options* o) {
 }
 
 void dev_reinit(DevVolume& v, double*& data, const Grid* g, const Options* o) {
+  PhaseTimer pt(v, PH_REINIT);
   const Box& b = v.box;
   const double dx = g->dx[0], dy = g->dx[1], dz = g->dx[2];
   const double dt_r = 0.5 * g->dx[0];
@@ -119,6 +120,7 @@ void dev_reinit(DevVolume& v, double*& data, const Grid* g, const Options* o) {
 // trapComponents_mask (trapComponents.c:156-375)
 
 void dev_trap(DevVolume& v, const Grid* g, const Options* o) {
+  PhaseTimer pt(v, PH_TRAP);
   const int64_t n = v.n;
   if (o->phi_nw_ind < 0 || o->phi_nw_ind >= n || o->phi_w_ind < 0 || o->phi_w_ind >= n)
     throw Error(QSSGPU_ERR_ARG, "phi_nw_ind / phi_w_ind outside the grid (call getMainInd_new)");
@@ -136,6 +138,7 @@ void dev_trap(DevVolume& v, const Grid* g, const Options* o) {
 }
 
 double dev_volume(DevVolume& v, const double* f, const Grid* g, double eps) {
+  PhaseTimer pt(v, PH_REDUCE);
   launch_volume(v.stream, v.box, f, g->dx[0], g->dx[1], g->dx[2], eps, v.contrib, v.dscal);
   QSS_CK(cudaMemcpyAsync(v.h_scal, v.dscal, sizeof(double), cudaMemcpyDeviceToHost, v.stream));
   sync(v);
@@ -143,6 +146,7 @@ double dev_volume(DevVolume& v, const double* f, const Grid* g, double eps) {
 }
 
 double dev_maxnorm(DevVolume& v, const Options* o) {
+  PhaseTimer pt(v, PH_REDUCE);
   launch_maxnormdiff(v.stream, v.box, v.phi, v.phi_prev, o->err_check_zone, v.red + 2);
   unsigned long long key;
   QSS_CK(cudaMemcpyAsync(&key, v.red + 2, sizeof key, cudaMemcpyDeviceToHost, v.stream));
@@ -207,6 +211,7 @@ int kernels_per_step(int order, int mode) {
 // Runs the inner loop to completion; returns dt_sub.
 double dev_inner_loop(DevVolume& v, const SchemeSel& sc, const Options* o, const Grid* g, double a,
                       int max_steps) {
+  PhaseTimer pt(v, PH_INNER);
   const int nslabs = num_slabs_for(g);
   if (sc.scheme == ENO3 && g->jhi_fb - g->jlo_gb > g->khi_gb - g->klo_gb)
     throw Error(QSSGPU_ERR_UNSUPPORTED,
@@ -402,6 +407,7 @@ double constCurvModel3d(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out) {
   DevVolume& v = volume_for(p, g);
   if (scope.outermost()) {
     v.inner_steps = v.outer_iters = 0;
+    reset_phases(v);
     upload_for_const_curv(v, p, o, true);
   }
   double t = dev_const_curv(v, true, o, p, g, fp_out, 0.0);
@@ -417,12 +423,25 @@ double constCurvModel3dNoVar(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_ou
   DevVolume& v = volume_for(p, g);
   if (scope.outermost()) {
     v.inner_steps = v.outer_iters = 0;
+    reset_phases(v);
     upload_for_const_curv(v, p, o, false);
   }
   double t = dev_const_curv(v, false, o, p, g, fp_out, a);
   if (scope.outermost()) download_dirty(v, p);
   return t;
   QSS_API_END(return -1)
+}
+
+// host wall time of the last top-level call on p by phase: out[0] total,
+// [1] set-up, [2] uploads, [3] inner steps, [4] trapping, [5]
+// reinitialisation, [6] volume and max-norm reductions, [7] downloads
+void qssgpu_call_times(const QSS_DataArrays* p, const Grid* g, double* out) {
+  try {
+    DevVolume& v = volume_for(p, g);
+    for (int k = 0; k < 8; k++) out[k] = v.phase_s[k];
+  } catch (const Error& e) {
+    set_error(e.code, e.what());
+  }
 }
 
 // statistics of the last top-level call on p: inner steps and outer iterations

@@ -25,7 +25,7 @@ using namespace qss;
 namespace {
 
 cudaStream_t abi_stream() {
-  static cudaStream_t s = nullptr;
+  thread_local cudaStream_t s = nullptr;
   if (!s) QSS_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   return s;
 }
@@ -448,7 +448,8 @@ void qss3dvolumeregionphilessthanzero_(double* volume, const double* phi, GB6P, 
     return;
   }
   const size_t bytes = (size_t)bx.npts() * sizeof(double);
-  DBuf dp(bytes), dc((size_t)bx.fbx() * bx.fby() * bx.fbz() * sizeof(double)), dv(8);
+  DBuf dp(bytes), dc((size_t)volume_scratch_doubles((int64_t)bx.fbx() * bx.fby() * bx.fbz()) * sizeof(double)),
+      dv(8);
   h2d(dp, phi, bytes);
   launch_volume(abi_stream(), bx, dp.d(), *dx, *dy, *dz, *epsilon, dc.d(), dv.d());
   double v;

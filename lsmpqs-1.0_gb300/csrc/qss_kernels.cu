@@ -617,27 +617,6 @@ __global__ void k_vol_contrib(Box b, const double* __restrict__ phi, double dV, 
   }
 }
 
-// The reference accumulates the volume in loop order (qss_util3d.f:336-347).
-// Floating-point addition is not associative, so to return the identical
-// double the sum is formed in that order: one warp streams the
-// contributions, every lane runs the same dependent chain over the nonzero
-// ones (adding an exact zero leaves the sum unchanged).
-__global__ void k_vol_serial(const double* __restrict__ contrib, int64_t n, double* out) {
-  const int lane = threadIdx.x;
-  double v = 0.0;
-  for (int64_t base = 0; base < n; base += 32) {
-    const int64_t q = base + lane;
-    const double x = (q < n) ? contrib[q] : 0.0;
-    unsigned nz = __ballot_sync(0xffffffffu, x != 0.0);
-    while (nz) {
-      const int l = __ffs(nz) - 1;
-      nz &= nz - 1;
-      v = v + __shfl_sync(0xffffffffu, x, l);
-    }
-  }
-  if (lane == 0) *out = v;
-}
-
 // ---------------------------------------------------------------------------
 // geometry (src/geometry/qss_initialization3d.c:33-165, 440-522)
 
@@ -949,11 +928,11 @@ void launch_maxnormdiff(cudaStream_t s, const Box& b, const double* f1, const do
 }
 
 void launch_volume(cudaStream_t s, const Box& b, const double* phi, double dx, double dy, double dz, double eps,
-                   double* contrib, double* out) {
+                   double* scratch, double* out) {
   const int64_t n = (int64_t)b.fbx() * b.fby() * b.fbz();
   const double dV = dx * dy * dz;
-  k_vol_contrib<<<grid1(n), kBlk1, 0, s>>>(b, phi, dV, eps, contrib);
-  k_vol_serial<<<1, 32, 0, s>>>(contrib, n, out);
+  k_vol_contrib<<<grid1(n), kBlk1, 0, s>>>(b, phi, dV, eps, scratch);
+  launch_loop_sum(s, scratch, n, scratch + n, out);
 }
 
 void launch_sphere(cudaStream_t s, const Box& b, double* phi, const double* x_lo_gb, const double* dxv, double cx,

@@ -171,8 +171,15 @@ __host__ __device__ inline double key_to_double(unsigned long long k) {
 void launch_maxnormdiff(cudaStream_t s, const Box& b, const double* f1, const double* f2,
                         double zone, unsigned long long* key);
 // sequential (loop-order) smoothed volume of {phi < 0}; contrib is fill-box sized scratch
+// Smoothed volume of {phi < 0} summed in the reference's loop order;
+// scratch holds volume_scratch_doubles(fill-box voxels) doubles.
 void launch_volume(cudaStream_t s, const Box& b, const double* phi, double dx, double dy, double dz,
-                   double eps, double* contrib, double* out);
+                   double eps, double* scratch, double* out);
+// the sequentially rounded sum c[0] + c[1] + ... + c[n-1] (qss_volsum.cu);
+// scratch holds loop_sum_scratch_doubles(n) doubles
+int64_t loop_sum_scratch_doubles(int64_t n);
+void launch_loop_sum(cudaStream_t s, const double* c, int64_t n, double* scratch, double* out);
+inline int64_t volume_scratch_doubles(int64_t nfb) { return nfb + loop_sum_scratch_doubles(nfb); }
 
 // ---- geometry ------------------------------------------------------------
 void launch_sphere(cudaStream_t s, const Box& b, double* phi, const double* x_lo_gb, const double* dxv,

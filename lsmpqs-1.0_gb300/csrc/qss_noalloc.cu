@@ -18,10 +18,13 @@
 
 using namespace qss;
 
-// Largest fill box accepted: 2^21 voxels (128^3) -> 16 MiB of scratch per GPU.
+// Largest fill box accepted: 2^21 voxels (128^3) -> 16 MiB of scratch per GPU
+// (one contribution per voxel, plus 8 doubles per chunk of 4096 for the
+// parallel loop-order sum and 64 of padding).
 #define QSSGPU_NOALLOC_MAX_FB_VOXELS (1 << 21)
+#define QSSGPU_NOALLOC_SCRATCH_DOUBLES (QSSGPU_NOALLOC_MAX_FB_VOXELS + 8 * (QSSGPU_NOALLOC_MAX_FB_VOXELS / 4096) + 64)
 
-static __device__ __align__(256) double g_noalloc_contrib[QSSGPU_NOALLOC_MAX_FB_VOXELS];
+static __device__ __align__(256) double g_noalloc_contrib[QSSGPU_NOALLOC_SCRATCH_DOUBLES];
 
 namespace {
 
@@ -83,7 +86,11 @@ int qssgpu_volume_noalloc(const double* d_phi, const int gb[6], const int ib[6],
                                       std::to_string(QSSGPU_NOALLOC_MAX_FB_VOXELS) +
                                       "); use qss3dvolumeregionphilessthanzero_ for larger boxes");
     // Every scratch entry the sum reads is written first by the contribution
-    // kernel, so nothing has to be cleared between calls.
+    // and chunk kernels, so nothing has to be cleared between calls.
+    static_assert(QSSGPU_NOALLOC_SCRATCH_DOUBLES >= QSSGPU_NOALLOC_MAX_FB_VOXELS + 8 * ((QSSGPU_NOALLOC_MAX_FB_VOXELS + 4095) / 4096) + 64,
+                  "scratch below volume_scratch_doubles of the largest box");
+    if (volume_scratch_doubles(nfb) > QSSGPU_NOALLOC_SCRATCH_DOUBLES)
+      throw Error(QSSGPU_ERR_ARG, "qssgpu_volume_noalloc: scratch too small");
     launch_volume(s, b, d_phi, dx, dy, dz, epsilon, scratch, d_volume);
     QSS_CK(cudaGetLastError());
     return 0;

@@ -13,7 +13,11 @@
 #include <cstring>
 #include <initializer_list>
 #include <ctime>
+#include <atomic>
+#include <chrono>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "qss_fortran_abi.h"
 #include "qss_state.h"
@@ -32,6 +36,7 @@ void setSpaceDerivFunc(Grid* g, Options* o);
 void setThetaOverlap(QSS_DataArrays* p, Grid* g, Options* o);
 void getMainInd_new(Options* o, QSS_DataArrays* p, Grid* g);
 int qssgpu_last_error(void);
+const char* qssgpu_error_string(void);
 void qssgpu_clear_error(void);
 }
 
@@ -66,10 +71,17 @@ void dev_reservoir(DevVolume& v, const Grid* g) {
   launch_box(v.stream, v.box, v.phi_extra, g->x_lo_ghostbox, g->dx, corner, side, -1);
 }
 
-void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out, bool outermost) {
+// The per-step files are named prefix + "data_step_<k>" (the reference's
+// names for prefix ""); a null prefix writes none.
+void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out, bool outermost,
+                const char* prefix) {
   DevVolume& v = volume_for(p, g);
   if (outermost) {
     v.inner_steps = v.outer_iters = 0;
+    reset_phases(v);
+  }
+  PhaseTimer total(v, PH_TOTAL);
+  if (outermost) {
     upload(v, p, H_PHI);
     upload(v, p, H_MASK);
   }
@@ -139,11 +151,13 @@ void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out
     if (o->reservoir_inlet) launch_min_into(v.stream, n, v.phi, v.phi, v.phi_extra);
     launch_max_into(v.stream, n, v.phi, v.mask, v.phi);
     v.dirty[H_PHI] = true;
-    snprintf(fname, sizeof fname, "data_step_%d", step);
+    if (prefix) {
+      snprintf(fname, sizeof fname, "%sdata_step_%d", prefix, step);
+      QSS_CK(cudaMemcpyAsync(p->phi, v.phi, n * sizeof(double), cudaMemcpyDeviceToHost, v.stream));
+      QSS_CK(cudaStreamSynchronize(v.stream));
+      writeDataArrayQSS(p->phi, g, fname, GZIP);
+    }
     step += 1;
-    QSS_CK(cudaMemcpyAsync(p->phi, v.phi, n * sizeof(double), cudaMemcpyDeviceToHost, v.stream));
-    QSS_CK(cudaStreamSynchronize(v.stream));
-    writeDataArrayQSS(p->phi, g, fname, GZIP);
   }
   if (outermost) download_dirty(v, p);
 }
@@ -171,7 +185,7 @@ extern "C" {
 void drain_model3d(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out) {
   CallScope scope;
   QSS_API_BEGIN
-  dev_ladder(true, o, p, g, fp_out, scope.outermost());
+  dev_ladder(true, o, p, g, fp_out, scope.outermost(), "");
   QSS_API_END(return)
 }
 
@@ -179,8 +193,74 @@ void drain_model3d(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out) {
 void imbibe_model3d(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out) {
   CallScope scope;
   QSS_API_BEGIN
-  dev_ladder(false, o, p, g, fp_out, scope.outermost());
+  dev_ladder(false, o, p, g, fp_out, scope.outermost(), "");
   QSS_API_END(return)
+}
+
+// See include/lsmpqs_gpu.h.
+int qssgpu_ladder_batch(int drain, int n, Options* const* o, QSS_DataArrays* const* p, Grid* const* g,
+                        FILE* const* fp, const char* const* prefix, int workers) {
+  qssgpu_clear_error();
+  if (n < 0 || (n > 0 && (!o || !p || !g))) {
+    set_error(QSSGPU_ERR_ARG, "qssgpu_ladder_batch: bad arguments");
+    return n > 0 ? n : 1;
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < i; j++)
+      if (p[i] == p[j] || o[i] == o[j]) {
+        set_error(QSSGPU_ERR_ARG, "qssgpu_ladder_batch: volumes must not share arrays or options");
+        return n;
+      }
+  if (workers <= 0) workers = n;
+  if (workers > 64) workers = 64;
+  if (workers > n) workers = n;
+  std::atomic<int> next{0};
+  std::vector<int> codes(n, 0);
+  std::vector<std::string> msgs(n);
+  std::vector<double> setup(n, 0.0);
+  // device arrays of every volume first: allocation serialises the device,
+  // so it is done before the volumes run
+  for (int v = 0; v < n; v++) {
+    const auto t0 = std::chrono::steady_clock::now();
+    try {
+      volume_for(p[v], g[v]);
+    } catch (const Error& e) {
+      codes[v] = e.code ? e.code : 1;
+      msgs[v] = e.what();
+    }
+    setup[v] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  auto work = [&]() {
+    for (int v = next++; v < n; v = next++) {
+      if (codes[v]) continue;
+      qssgpu_clear_error();
+      try {
+        CallScope scope;  // each volume is an outermost call on its worker thread
+        dev_ladder(drain != 0, o[v], p[v], g[v], fp ? fp[v] : nullptr, true, prefix ? prefix[v] : nullptr);
+        volume_for(p[v], g[v]).phase_s[PH_SETUP] += setup[v];
+        QSS_CK(cudaStreamSynchronize(volume_for(p[v], g[v]).stream));
+      } catch (const Error& e) {
+        set_error(e.code, e.what());
+      } catch (const std::exception& e) {
+        set_error(QSSGPU_ERR_CUDA, e.what());
+      }
+      codes[v] = qssgpu_last_error();
+      if (codes[v]) msgs[v] = qssgpu_error_string();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < workers; w++) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  int failed = 0, first = -1;
+  for (int v = 0; v < n; v++)
+    if (codes[v]) {
+      failed++;
+      if (first < 0) first = v;
+    }
+  qssgpu_clear_error();
+  if (first >= 0) set_error(codes[first], "volume " + std::to_string(first) + ": " + msgs[first]);
+  return failed;
 }
 
 static int top_level(bool drain, Options* o, char* fdata, char* fgrid, char* fmask) {
@@ -300,7 +380,7 @@ void reinitializeSubcellFix3d(double* data, Grid* g, Options* o) {
   QSS_API_BEGIN
   ensure_device();
   // a private device volume keyed by the host array
-  static QSS_DataArrays key;
+  thread_local QSS_DataArrays key;
   DevVolume& v = volume_for(&key, g);
   QSS_CK(cudaMemcpyAsync(v.scratch, data, v.n * sizeof(double), cudaMemcpyHostToDevice, v.stream));
   double* d = v.scratch;
@@ -325,7 +405,7 @@ void signedLinearExtrapolationBCqss(double* phi, Grid* g, int idx) {
     case 9: for (int f = 0; f < 6; f++) faces[nf++] = f; break;
     default: return;
   }
-  static QSS_DataArrays key;
+  thread_local QSS_DataArrays key;
   DevVolume& v = volume_for(&key, g);
   QSS_CK(cudaMemcpyAsync(v.scratch, phi, v.n * sizeof(double), cudaMemcpyHostToDevice, v.stream));
   for (int q = 0; q < nf; q++) launch_face(v.stream, v.box, v.scratch, faces[q]);
@@ -366,7 +446,7 @@ void setThetaOverlap(QSS_DataArrays* p, Grid* g, Options* o) {
 // qss_general_util.c:711-728 -- data is a host array
 void initializeDisconnectedMasks(double* data, Grid* g) {
   QSS_API_BEGIN
-  static QSS_DataArrays key;
+  thread_local QSS_DataArrays key;
   DevVolume& v = volume_for(&key, g);
   dev_init_disconnected(v, v.scratch, g);
   QSS_CK(cudaMemcpyAsync(data, v.scratch, v.n * sizeof(double), cudaMemcpyDeviceToHost, v.stream));

@@ -1,4 +1,6 @@
 // qss_state.cu -- device state per QSS_DataArrays, host<->device transfers, errors.
+#include <atomic>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <initializer_list>
@@ -12,14 +14,52 @@ namespace qss {
 thread_local int CallScope::depth = 0;
 
 namespace {
-int g_err = QSSGPU_OK;
-char g_msg[1024] = "";
+// error state of the calling thread (the batch entry point reports the
+// errors of its worker threads on the caller's)
+thread_local int g_err = QSSGPU_OK;
+thread_local char g_msg[1024] = "";
 std::mutex g_mu;
 std::unordered_map<const QSS_DataArrays*, DevVolume*> g_table;
 int g_slabs_override = 0;
 int g_weno_split = -1;  // -1: from the environment
 int g_emu_level = -1;   // -1: from the environment
 }  // namespace
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+PhaseTimer::PhaseTimer(DevVolume& vol, int phase) : v(&vol), ph(phase), t0(0) {
+  if (v->phase_open >= 0 && phase != PH_TOTAL) {
+    v = nullptr;  // nested: counted in the enclosing phase
+    return;
+  }
+  if (phase != PH_TOTAL) v->phase_open = phase;
+  t0 = now_s();
+}
+
+// $QSSGPU_PHASE_SYNC=1 makes every phase end with a stream synchronisation,
+// so that asynchronous device work is charged to the phase that queued it
+// (diagnostic timing; off by default)
+static bool phase_sync() {
+  static const int on = [] {
+    const char* e = getenv("QSSGPU_PHASE_SYNC");
+    return e && atoi(e) == 1 ? 1 : 0;
+  }();
+  return on != 0;
+}
+
+PhaseTimer::~PhaseTimer() {
+  if (!v) return;
+  if (phase_sync()) cudaStreamSynchronize(v->stream);
+  v->phase_s[ph] += now_s() - t0;
+  if (ph != PH_TOTAL) v->phase_open = -1;
+}
+
+void reset_phases(DevVolume& v) {
+  for (double& t : v.phase_s) t = 0;
+  v.phase_open = -1;
+}
 
 void set_error(int code, const std::string& msg) {
   g_err = code;
@@ -33,8 +73,8 @@ void clear_error() {
 }
 
 void ensure_device() {
-  static int state = -1;  // -1 unknown, 0 none, 1 ok
-  if (state == 1) return;
+  static std::atomic<int> state{-1};  // -1 unknown, 0 none, 1 ok
+  if (state.load() == 1) return;
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0) {
@@ -158,7 +198,7 @@ DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g) {
     dalloc(v->dplus[d], n);
     dalloc(v->dminus[d], n);
   }
-  dalloc(v->contrib, v->nfb);
+  dalloc(v->contrib, volume_scratch_doubles(v->nfb));
   dalloc(v->labels, n);
   dalloc(v->nsrc, n);
   dalloc(v->bin, n);
@@ -259,6 +299,7 @@ static bool usable(const void* h) {
 }
 
 void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which) {
+  PhaseTimer pt(v, PH_UPLOAD);
   void* h = host_ptr(p, which);
   void* d = dev_ptr(v, which);
   if (!usable(h) || !d) throw Error(QSSGPU_ERR_ARG, "input array is not allocated");
@@ -266,6 +307,7 @@ void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which) {
 }
 
 void download_dirty(DevVolume& v, QSS_DataArrays* p) {
+  PhaseTimer pt(v, PH_DOWNLOAD);
   for (int a = 0; a < H_COUNT; a++) {
     HostArray w = (HostArray)a;
     void* h = host_ptr(p, w);

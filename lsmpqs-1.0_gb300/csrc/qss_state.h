@@ -64,7 +64,7 @@ struct DevVolume {
   double *vel_n = nullptr, *bcoef = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr;
   double *scratch = nullptr;                           // trapped-phase work array
   double *r_phi0 = nullptr, *r_dist = nullptr, *r_next = nullptr;  // reinitialisation
-  double *contrib = nullptr;                           // volume contributions (fill box)
+  double *contrib = nullptr;                           // volume contributions (fill box) + sum scratch
   double *dplus[3] = {}, *dminus[3] = {};              // WENO5 one-sided derivatives per axis
   int *labels = nullptr, *nsrc = nullptr, *rowlast = nullptr, *carry = nullptr;
   unsigned char* bin = nullptr;
@@ -85,6 +85,9 @@ struct DevVolume {
   // statistics of the last top-level call
   long long inner_steps = 0;
   long long outer_iters = 0;
+  // host wall time per phase of the last top-level call (PhaseTimer)
+  double phase_s[8] = {};
+  int phase_open = -1;
 };
 
 DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g);
@@ -106,6 +109,18 @@ int weno_mode();
 int emu_level();
 
 // nesting depth of API calls: only the outermost call moves host data
+// Host wall-time accounting of one volume's top-level call, by phase; a
+// phase opened inside another is counted in the outer one only.
+enum Phase { PH_TOTAL = 0, PH_SETUP, PH_UPLOAD, PH_INNER, PH_TRAP, PH_REINIT, PH_REDUCE, PH_DOWNLOAD };
+struct PhaseTimer {
+  DevVolume* v;
+  int ph;
+  double t0;
+  PhaseTimer(DevVolume& vol, int phase);
+  ~PhaseTimer();
+};
+void reset_phases(DevVolume& v);
+
 struct CallScope {
   static thread_local int depth;
   CallScope() { depth++; }

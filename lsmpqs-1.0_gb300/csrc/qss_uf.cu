@@ -7,9 +7,12 @@
 // That label is a property of the component, not of the visiting order, so a
 // concurrent union-find that keeps the same rule (link the smaller root under
 // the larger, by compare-and-swap on the root) produces identical labels:
-//   1. parent[v] = v for every foreground voxel;
-//   2. each voxel unites with its 13 neighbours that precede it in linear
-//      order (the other 13 of the 26 are covered from the other side);
+//   1. per 8x8x8 tile, in shared memory: every foreground voxel unites with
+//      its preceding neighbours inside the tile; parent[v] = the global index
+//      of v's tile-local root (0 for background);
+//   2. voxels on a tile face unite, in global memory, with their preceding
+//      neighbours in other tiles (every adjacent pair is a preceding pair
+//      from one side);
 //   3. labels[v] = root(v), 0 for background.
 // Every write to parent[] increases it (hooking a root under a larger root,
 // or compressing a node to a larger ancestor), so parent[x] > x holds for
@@ -71,36 +74,142 @@ __device__ __forceinline__ void unite(int* parent, int a, int b, int* err) {
   }
 }
 
-__global__ void k_uf_init(int64_t n, const unsigned char* __restrict__ bin, int* parent) {
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-    parent[q] = bin[q] ? (int)q : 0;
+// Tiles of 8 x 8 x 8 voxels: inside a tile the union-find runs in shared
+// memory (same rule: the smaller root is hung under the larger, so the local
+// root is the tile component's largest index, and the local order of a tile
+// is the global linear order restricted to it); then every voxel's global
+// parent is the global index of its local root (depth 1), and only the
+// adjacencies that cross a tile face are united in global memory.
+constexpr int kTile = 8;
+constexpr int kTileN = kTile * kTile * kTile;
+constexpr int kTileThreads = 256;
+
+__device__ __forceinline__ int lfind(int* lp, int x, int* err) {
+  int r = x;
+  int it = 0;
+  while (true) {
+    const int p = lp[r];
+    if (p == r) break;
+    r = p;
+    if (++it > kTileN) {
+      *err |= ERR_UF_LIMIT;
+      return r;
+    }
+  }
+  int y = x;
+  it = 0;
+  while (y < r && it++ < kTileN) {  // compression upwards only (see find_root)
+    const int p = lp[y];
+    if (p < r) lp[y] = r;
+    y = p;
+  }
+  return r;
 }
 
-__global__ void k_uf_hook(Box b, const unsigned char* __restrict__ bin, int* parent, Ctl* ctl) {
-  const int64_t n = b.npts();
+__device__ __forceinline__ void lunite(int* lp, int a, int b, int* err) {
+  int ra = lfind(lp, a, err), rb = lfind(lp, b, err);
+  int it = 0;
+  while (ra != rb) {
+    if (ra > rb) {
+      const int t = ra;
+      ra = rb;
+      rb = t;
+    }
+    const int old = atomicCAS(&lp[ra], ra, rb);
+    if (old == ra) return;
+    ra = lfind(lp, old, err);
+    rb = lfind(lp, rb, err);
+    if (++it > 4 * kTileN) {
+      *err |= ERR_UF_LIMIT;
+      return;
+    }
+  }
+}
+
+// offsets of the 13 neighbours that precede a voxel in linear order
+__device__ __forceinline__ void back_offset(int m, int& di, int& dj, int& dk) {
+  if (m < 9) {
+    dk = -1;
+    dj = m / 3 - 1;
+    di = m % 3 - 1;
+  } else if (m < 12) {
+    dk = 0;
+    dj = -1;
+    di = m - 10;
+  } else {
+    dk = 0;
+    dj = 0;
+    di = -1;
+  }
+}
+
+// tile-local labelling; writes parent[] for every voxel of the tile
+// (background 0, foreground the global index of its local root)
+__global__ void __launch_bounds__(kTileThreads) k_uf_tile(Box b, const unsigned char* __restrict__ bin, int* parent,
+                                                          Ctl* ctl) {
+  __shared__ int lp[kTileN];
+  __shared__ unsigned char lb[kTileN];
+  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile, z0 = blockIdx.z * kTile;
   int err = 0;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    if (!bin[q]) continue;
-    const int i = (int)(q % b.nx);
-    const int64_t r = q / b.nx;
-    const int j = (int)(r % b.ny), k = (int)(r / b.ny);
-    // the 13 neighbours with a smaller linear index
+  for (int l = threadIdx.x; l < kTileN; l += kTileThreads) {
+    const int li = l % kTile, lj = (l / kTile) % kTile, lk = l / (kTile * kTile);
+    const int i = x0 + li, j = y0 + lj, k = z0 + lk;
+    const bool in = i < b.nx && j < b.ny && k < b.nz;
+    const unsigned char v = in ? bin[b.idx(i, j, k)] : 0;
+    lb[l] = v;
+    lp[l] = l;
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < kTileN; l += kTileThreads) {
+    if (!lb[l]) continue;
+    const int li = l % kTile, lj = (l / kTile) % kTile, lk = l / (kTile * kTile);
 #pragma unroll
     for (int m = 0; m < 13; m++) {
       int di, dj, dk;
-      if (m < 9) {
-        dk = -1;
-        dj = m / 3 - 1;
-        di = m % 3 - 1;
-      } else if (m < 12) {
-        dk = 0;
-        dj = -1;
-        di = m - 10;
-      } else {
-        dk = 0;
-        dj = 0;
-        di = -1;
-      }
+      back_offset(m, di, dj, dk);
+      const int a = li + di, c = lj + dj, d = lk + dk;
+      if (a < 0 || c < 0 || d < 0 || a >= kTile || c >= kTile) continue;
+      const int l2 = a + kTile * (c + kTile * d);
+      if (lb[l2]) lunite(lp, l, l2, &err);
+    }
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < kTileN; l += kTileThreads) {
+    const int li = l % kTile, lj = (l / kTile) % kTile, lk = l / (kTile * kTile);
+    const int i = x0 + li, j = y0 + lj, k = z0 + lk;
+    if (i >= b.nx || j >= b.ny || k >= b.nz) continue;
+    int g = 0;
+    if (lb[l]) {
+      const int r = lfind(lp, l, &err);
+      const int ri = r % kTile, rj = (r / kTile) % kTile, rk = r / (kTile * kTile);
+      g = (int)b.idx(x0 + ri, y0 + rj, z0 + rk);
+    }
+    parent[b.idx(i, j, k)] = g;
+  }
+  if (err && ctl) atomicOr(&ctl->err, err);
+}
+
+// unions across tile faces: each voxel on a low face of its tile with its
+// preceding neighbours in other tiles
+__global__ void __launch_bounds__(kTileThreads) k_uf_cross(Box b, const unsigned char* __restrict__ bin, int* parent,
+                                                           Ctl* ctl) {
+  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile, z0 = blockIdx.z * kTile;
+  int err = 0;
+  for (int l = threadIdx.x; l < kTileN; l += kTileThreads) {
+    const int li = l % kTile, lj = (l / kTile) % kTile, lk = l / (kTile * kTile);
+    // preceding offsets have di, dj in {-1, 0, 1} and dk in {-1, 0}: only
+    // these voxels have one outside the tile
+    if (li != 0 && li != kTile - 1 && lj != 0 && lj != kTile - 1 && lk != 0) continue;
+    const int i = x0 + li, j = y0 + lj, k = z0 + lk;
+    if (i >= b.nx || j >= b.ny || k >= b.nz) continue;
+    const int64_t q = b.idx(i, j, k);
+    if (!bin[q]) continue;
+#pragma unroll
+    for (int m = 0; m < 13; m++) {
+      int di, dj, dk;
+      back_offset(m, di, dj, dk);
+      const int a = li + di, c = lj + dj, d = lk + dk;
+      if (a >= 0 && c >= 0 && d >= 0 && a < kTile && c < kTile) continue;  // same tile: done
       const int i2 = i + di, j2 = j + dj, k2 = k + dk;
       if (i2 < 0 || j2 < 0 || k2 < 0 || i2 >= b.nx || j2 >= b.ny) continue;
       const int64_t q2 = b.idx(i2, j2, k2);
@@ -217,8 +326,9 @@ unsigned grid_for(int64_t n) {
 
 void launch_label(cudaStream_t s, const Box& b, const unsigned char* bin, int* labels, Ctl* ctl) {
   const int64_t n = b.npts();
-  k_uf_init<<<grid_for(n), 256, 0, s>>>(n, bin, labels);
-  k_uf_hook<<<grid_for(n), 256, 0, s>>>(b, bin, labels, ctl);
+  const dim3 tiles((b.nx + kTile - 1) / kTile, (b.ny + kTile - 1) / kTile, (b.nz + kTile - 1) / kTile);
+  k_uf_tile<<<tiles, kTileThreads, 0, s>>>(b, bin, labels, ctl);
+  k_uf_cross<<<tiles, kTileThreads, 0, s>>>(b, bin, labels, ctl);
   k_uf_final<<<grid_for(n), 256, 0, s>>>(n, bin, labels, ctl);
 }
 
