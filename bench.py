@@ -399,6 +399,71 @@ def batched_arm(args):
                     "after the other, batched = all volumes in one qssgpu_ladder_batch call"}
 
 
+def adjoint_arm(args):
+    """Adjoint mode: 128^3 sphere pack (seed 3, radius 6 voxels, porosity 0.35),
+    contact angle = trilinear interpolation of an 8^3 control grid in 0..60
+    degrees (seed 3), target = H_eps(phi_T) of a hidden control grid (seed 4),
+    TVD-RK3 WENO5 steps at curvature 0.2 per voxel, checkpoints every 20 steps.
+    Reports the wall-clock ratio of forward + gradient to forward alone."""
+    lib = Q.load(Q.GPU_LIB)
+    n, steps, ckpt = args.adj_n, args.adj_steps, args.adj_ckpt
+    g = Q.make_grid(lib, n)
+    v = Q.Volume(g)
+    m = S.overlapping(n, radius_vox=6.0, porosity=0.35, seed=3).mask()
+    v["mask"][...] = m
+    v["phi"][...] = S.initial_phi(m, n)
+    o = Q.default_options(lib)
+    dx = g.dx[0]
+    o.a, o.b, o.overlap = 0.2 / dx, 0.04, 0.0
+    dt = 0.5 / (2 * o.b * 3 / dx ** 2 + 2.0 / dx + abs(o.a) * math.sqrt(3) / dx)
+
+    def angles(seed):
+        c = np.random.default_rng(seed).uniform(0.0, math.radians(60.0), (8, 8, 8))
+        t = np.arange(n) / (n - 1) * 7
+        i0 = np.minimum(np.floor(t).astype(int), 6)
+        f = t - i0
+        out = np.zeros((n, n, n))
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dxx in (0, 1):
+                    w = (np.where(dz, f, 1 - f)[:, None, None] * np.where(dy, f, 1 - f)[None, :, None] *
+                         np.where(dxx, f, 1 - f)[None, None, :])
+                    out += w * c[np.ix_(i0 + dz, i0 + dy, i0 + dxx)]
+        full = np.zeros(v["mask"].shape)
+        full[3:n + 3, 3:n + 3, 3:n + 3] = out
+        return full
+
+    theta, hidden = angles(3), angles(4)
+    zeros = np.zeros(v["mask"].shape)
+    loss = C.c_double(0)
+    phiT = np.zeros(v["mask"].shape)
+    if lib.qssgpu_forward_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(hidden), Q.dptr(zeros), steps, dt,
+                                C.byref(loss), Q.dptr(phiT)):
+        Q.check(lib)
+    eps = 1.5 * dx
+    target = np.where(phiT < -eps, 0.0, np.where(phiT > eps, 1.0, 0.5 + phiT / (2 * eps) +
+                                                  np.sin(math.pi * phiT / eps) / (2 * math.pi)))
+    # warm-up, then timed forward and forward + gradient
+    lib.qssgpu_forward_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(theta), Q.dptr(target), 2, dt,
+                             C.byref(loss), None)
+    t0 = time.perf_counter()
+    if lib.qssgpu_forward_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(theta), Q.dptr(target), steps, dt,
+                                C.byref(loss), None):
+        Q.check(lib)
+    t_fwd = time.perf_counter() - t0
+    grad = np.zeros(v["mask"].shape)
+    t0 = time.perf_counter()
+    if lib.qssgpu_adjoint_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(theta), Q.dptr(target), steps, dt,
+                                ckpt, C.byref(loss), Q.dptr(grad)):
+        Q.check(lib)
+    t_adj = time.perf_counter() - t0
+    return {"n": n, "steps": steps, "checkpoint_every": ckpt, "loss": loss.value,
+            "forward_s": t_fwd, "forward_and_gradient_s": t_adj, "adjoint_cost_over_forward": t_adj / t_fwd,
+            "forward_voxel_steps_per_s": n ** 3 * steps / t_fwd,
+            "grad_abs_max": float(np.abs(grad).max()),
+            "note": "wall clock including uploads; gradient d loss / d theta per voxel (radians)"}
+
+
 def cpu_arm(args, nz: int, steps: int, warmup: int, threads: int):
     """The reference algorithm on the host cores (CPU oracle, OpenMP) on a
     512 x 512 x nz slab of the workload; returns voxel-steps/s and details."""
@@ -442,6 +507,11 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--batch-workers", type=int, default=0)
     ap.add_argument("--batch-only", action="store_true", help="measure batched mode only")
+    ap.add_argument("--adjoint", action="store_true", help="also measure the adjoint mode (128^3)")
+    ap.add_argument("--adjoint-only", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=128)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--adj-ckpt", type=int, default=20)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per stage launch from an ncu capture (optional)")
     args = ap.parse_args()
@@ -470,6 +540,11 @@ def main():
         dist.close()
         return
 
+    if args.adjoint_only:
+        if dist.rank == 0:
+            print(json.dumps({"adjoint_mode": adjoint_arm(args)}))
+        dist.close()
+        return
     if args.batch_only:
         if dist.rank == 0:
             print(json.dumps({"batched_mode": batched_arm(args)}))
@@ -492,6 +567,8 @@ def main():
                 "cpu_baseline": cpu, "clocks": res["clocks"]}
         if args.batched:
             line["batched_mode"] = batched_arm(args)
+        if args.adjoint:
+            line["adjoint_mode"] = adjoint_arm(args)
         print(json.dumps(line))
     dist.close()
 

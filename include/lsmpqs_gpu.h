@@ -230,6 +230,23 @@ int qssgpu_set_emu_level(int level);
    failed; qssgpu_last_error / qssgpu_error_string then describe the first. */
 int qssgpu_ladder_batch(int drain, int n, Options *const *o, QSS_DataArrays *const *p, Grid *const *g,
                         FILE *const *fp, const char *const *prefix, int workers);
+/* Adjoint mode (no reference counterpart).  Forward model: nsteps TVD-RK3
+   steps of the variable-coefficient WENO5 update of constCurvModel3d with a
+   fixed time step dt (no connectivity, reinitialisation or CFL), starting from
+   p->phi, with the normal speed of setVarNorm3dTheta for the per-voxel contact
+   angle theta[] (radians, ghost-box array; a0 = o->a, curvature coefficient
+   o->b, imposition of p->mask - o->overlap); loss = sum over the fill box of
+   (H_eps(phi_T) - target)^2, eps = 1.5 dx, H the reference's smoothed
+   Heaviside, target a ghost-box array.  qssgpu_adjoint_theta returns the loss
+   and d loss / d theta (ghost-box array, zero on the ghost layers) by a
+   hand-written reverse pass that recomputes the states from checkpoints every
+   ckpt steps (ckpt <= 0: one segment); qssgpu_forward_theta only the loss
+   (and phi_T into phi_out, a ghost-box array, when phi_out is not NULL).
+   Host arrays are read, not modified.  0 on success. */
+int qssgpu_adjoint_theta(Options *o, QSS_DataArrays *p, Grid *g, const double *theta, const double *target,
+                         int nsteps, double dt, int ckpt, double *loss, double *grad_theta);
+int qssgpu_forward_theta(Options *o, QSS_DataArrays *p, Grid *g, const double *theta, const double *target,
+                         int nsteps, double dt, double *loss, double *phi_out);
 /* The sequentially rounded sum values[0] + values[1] + ... + values[n-1]
    (a plain C loop's result, bit for bit) computed on the GPU: in parallel
    by binade-wise integer sums for non-negative runs, element by element

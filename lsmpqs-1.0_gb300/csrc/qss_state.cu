@@ -112,6 +112,8 @@ static void check_grid(const Grid* g) {
   if (b.npts() >= (int64_t)INT32_MAX) throw Error(QSSGPU_ERR_ARG, "ghost box exceeds 2^31 points");
 }
 
+void validate_grid(const Grid* g) { check_grid(g); }
+
 int num_slabs_for(const Grid* g) {
   int t = g_slabs_override;
   if (t <= 0) {

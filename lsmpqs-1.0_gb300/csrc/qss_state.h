@@ -98,6 +98,8 @@ void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which);
 void download_dirty(DevVolume& v, QSS_DataArrays* p);
 
 int num_slabs_for(const Grid* g);
+// throws unless g is a 3-D grid the device path supports (>= 3 ghost layers)
+void validate_grid(const Grid* g);
 // WENO5 variable-coefficient stages: 0 one fused kernel per stage, 1 (default)
 // one kernel per axis + a combine kernel ($QSSGPU_WENO_MODE,
 // qssgpu_set_weno_split); both give identical results

@@ -165,6 +165,10 @@ def load(path: str) -> C.CDLL:
         "qssgpu_set_emu_level": (C.c_int, [C.c_int]),
         "qssgpu_call_times": (None, [P(QSSDataArrays), P(Grid), P(C.c_double)]),
         "qssgpu_loop_sum": (C.c_int, [P(C.c_double), C.c_longlong, P(C.c_double)]),
+        "qssgpu_adjoint_theta": (C.c_int, [P(Options), P(QSSDataArrays), P(Grid), P(C.c_double), P(C.c_double),
+                                           C.c_int, C.c_double, C.c_int, P(C.c_double), P(C.c_double)]),
+        "qssgpu_forward_theta": (C.c_int, [P(Options), P(QSSDataArrays), P(Grid), P(C.c_double), P(C.c_double),
+                                           C.c_int, C.c_double, P(C.c_double), P(C.c_double)]),
         "qssgpu_ladder_batch": (C.c_int, [C.c_int, C.c_int, P(P(Options)), P(P(QSSDataArrays)), P(P(Grid)),
                                           P(_PTR), P(C.c_char_p), C.c_int]),
         "qssgpu_emu_selftest": (C.c_int, [C.c_longlong, C.c_ulonglong, P(C.c_longlong), P(C.c_double)]),
