@@ -502,12 +502,13 @@ def main():
     ap.add_argument("--cpu-nz", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--fp64-peak", type=float, default=1.25)
-    ap.add_argument("--batched", action="store_true", help="also measure batched mode (uneven volumes)")
-    ap.add_argument("--batch-volumes", type=int, default=64)
-    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the batched-mode measurement (uneven volumes)")
+    ap.add_argument("--batch-volumes", type=int, default=16)
+    ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-workers", type=int, default=0)
     ap.add_argument("--batch-only", action="store_true", help="measure batched mode only")
-    ap.add_argument("--adjoint", action="store_true", help="also measure the adjoint mode (128^3)")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint-mode measurement")
     ap.add_argument("--adjoint-only", action="store_true")
     ap.add_argument("--adj-n", type=int, default=128)
     ap.add_argument("--adj-steps", type=int, default=200)

@@ -35,6 +35,16 @@ def oracle():
     return lib
 
 
+@pytest.fixture(autouse=True)
+def _oracle_one_thread(request):
+    """The reference's CFL step depends on the OpenMP thread count; other
+    libraries in the process (torch) may resize the shared OpenMP pool, so
+    every test that uses the oracle starts it on one thread."""
+    if "oracle" in request.fixturenames:
+        request.getfixturevalue("oracle").oracle_set_threads(1)
+    yield
+
+
 @pytest.fixture(scope="session")
 def ref():
     import qssgpu as Q
