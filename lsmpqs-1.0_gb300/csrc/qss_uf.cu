@@ -189,31 +189,49 @@ __global__ void __launch_bounds__(kTileThreads) k_uf_tile(Box b, const unsigned 
   if (err && ctl) atomicOr(&ctl->err, err);
 }
 
-// unions across tile faces: each voxel on a low face of its tile with its
-// preceding neighbours in other tiles
+// unions across tile faces: each voxel on a face of its tile with its
+// preceding neighbours in other tiles.  Neighbouring voxels mostly join the
+// same two tile components, so the lanes of a warp first agree on distinct
+// (parent, parent) pairs and only one lane per pair unites them (the parents
+// are in the same sets as the voxels).
 __global__ void __launch_bounds__(kTileThreads) k_uf_cross(Box b, const unsigned char* __restrict__ bin, int* parent,
                                                            Ctl* ctl) {
   const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile, z0 = blockIdx.z * kTile;
+  const unsigned lane = threadIdx.x & 31u;
   int err = 0;
+  // every thread runs kTileN / kTileThreads iterations (warp-uniform loop)
   for (int l = threadIdx.x; l < kTileN; l += kTileThreads) {
     const int li = l % kTile, lj = (l / kTile) % kTile, lk = l / (kTile * kTile);
     // preceding offsets have di, dj in {-1, 0, 1} and dk in {-1, 0}: only
     // these voxels have one outside the tile
-    if (li != 0 && li != kTile - 1 && lj != 0 && lj != kTile - 1 && lk != 0) continue;
+    const bool face = li == 0 || li == kTile - 1 || lj == 0 || lj == kTile - 1 || lk == 0;
     const int i = x0 + li, j = y0 + lj, k = z0 + lk;
-    if (i >= b.nx || j >= b.ny || k >= b.nz) continue;
-    const int64_t q = b.idx(i, j, k);
-    if (!bin[q]) continue;
-#pragma unroll
+    const bool in = i < b.nx && j < b.ny && k < b.nz;
+    const int64_t q = in ? b.idx(i, j, k) : 0;
+    const bool fg = face && in && bin[q];
+#pragma unroll 1
     for (int m = 0; m < 13; m++) {
       int di, dj, dk;
       back_offset(m, di, dj, dk);
-      const int a = li + di, c = lj + dj, d = lk + dk;
-      if (a >= 0 && c >= 0 && d >= 0 && a < kTile && c < kTile) continue;  // same tile: done
-      const int i2 = i + di, j2 = j + dj, k2 = k + dk;
-      if (i2 < 0 || j2 < 0 || k2 < 0 || i2 >= b.nx || j2 >= b.ny) continue;
-      const int64_t q2 = b.idx(i2, j2, k2);
-      if (bin[q2]) unite(parent, (int)q, (int)q2, &err);
+      int ra = -1, rb = -1;
+      if (fg) {
+        const int a = li + di, c = lj + dj, d = lk + dk;
+        const bool other_tile = !(a >= 0 && c >= 0 && d >= 0 && a < kTile && c < kTile);
+        const int i2 = i + di, j2 = j + dj, k2 = k + dk;
+        if (other_tile && i2 >= 0 && j2 >= 0 && k2 >= 0 && i2 < b.nx && j2 < b.ny) {
+          const int64_t q2 = b.idx(i2, j2, k2);
+          if (bin[q2]) {
+            ra = __ldcg(parent + q);
+            rb = __ldcg(parent + q2);
+          }
+        }
+      }
+      const bool pair = ra >= 0 && ra != rb;
+      const unsigned lo = (unsigned)(ra < rb ? ra : rb), hi = (unsigned)(ra < rb ? rb : ra);
+      const unsigned long long key =
+          pair ? (((unsigned long long)lo << 32) | hi) : (0xffffffff00000000ull | lane);
+      const unsigned peers = __match_any_sync(0xffffffffu, key);
+      if (pair && (unsigned)(__ffs(peers) - 1) == lane) unite(parent, ra, rb, &err);
     }
   }
   if (err && ctl) atomicOr(&ctl->err, err);
