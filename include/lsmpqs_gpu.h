@@ -230,6 +230,29 @@ int qssgpu_set_emu_level(int level);
    failed; qssgpu_last_error / qssgpu_error_string then describe the first. */
 int qssgpu_ladder_batch(int drain, int n, Options *const *o, QSS_DataArrays *const *p, Grid *const *g,
                         FILE *const *fp, const char *const *prefix, int workers);
+/* ---- pre- and post-processing on the GPU ---- */
+/* qss_general_util.h: reinitialisation of p->mask (tmax_r / (0.5 dx)
+   subcell-fix iterations); like the reference it leaves distance0 in
+   scratch1, the initial mask in scratch2, the last RHS in lse_rhs (fill box)
+   and the last iterate in phi_next */
+void qss_reinitialize_mask(QSS_DataArrays *p, Grid *g, Options *o);
+/* createMaskUBC (src/applications/createMaskUBC.c:76-112) as a library call:
+   p->mask = +dx where the 8-bit fill-box image (x fastest) is 255 (grain),
+   -dx elsewhere, zero on the ghost layers, then qss_reinitialize_mask;
+   dx = o->dx as in the reference */
+int qssgpu_create_mask_ubc(const unsigned char *ubc, QSS_DataArrays *p, Grid *g, Options *o);
+/* createInitFromMask (createInitFromMask.c:55-85, 3-D): p->phi = max(p->mask,
+   the inlet sphere of the reference: radius 0.7 (x_hi - x_lo) centred 0.7
+   radius before x_lo, or radius 90 dx at the centre with o->center_inlet) */
+int qssgpu_create_init_from_mask(QSS_DataArrays *p, Grid *g, Options *o);
+/* makeDiffSteps (makeDiffSteps.c:54-132, 3-D): diff = max(-step_a, step_b -
+   dx/2) (the lens between two saved steps), 26-connected labels of {diff < 0}
+   with inlet and outlet slabs, *percolates = inlet and outlet connected;
+   when it percolates and connected != NULL, connected = diff with the
+   non-wetting voxels outside the percolating component flipped.  Ghost-box
+   arrays. */
+int qssgpu_diff_steps(const double *step_a, const double *step_b, Grid *g, double *diff, double *connected,
+                      int *percolates);
 /* Adjoint mode (no reference counterpart).  Forward model: nsteps TVD-RK3
    steps of the variable-coefficient WENO5 update of constCurvModel3d with a
    fixed time step dt (no connectivity, reinitialisation or CFL), starting from

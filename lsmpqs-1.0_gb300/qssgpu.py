@@ -165,6 +165,15 @@ def load(path: str) -> C.CDLL:
         "qssgpu_set_emu_level": (C.c_int, [C.c_int]),
         "qssgpu_call_times": (None, [P(QSSDataArrays), P(Grid), P(C.c_double)]),
         "qssgpu_loop_sum": (C.c_int, [P(C.c_double), C.c_longlong, P(C.c_double)]),
+        "qss_reinitialize_mask": (None, [P(QSSDataArrays), P(Grid), P(Options)]),
+        "qssgpu_create_mask_ubc": (C.c_int, [P(C.c_ubyte), P(QSSDataArrays), P(Grid), P(Options)]),
+        "qssgpu_create_init_from_mask": (C.c_int, [P(QSSDataArrays), P(Grid), P(Options)]),
+        "qssgpu_diff_steps": (C.c_int, [P(C.c_double), P(C.c_double), P(Grid), P(C.c_double), P(C.c_double),
+                                        P(C.c_int)]),
+        "oracle_create_mask_ubc": (C.c_int, [P(C.c_ubyte), P(QSSDataArrays), P(Grid), P(Options)]),
+        "oracle_create_init_from_mask": (C.c_int, [P(QSSDataArrays), P(Grid), P(Options)]),
+        "oracle_diff_steps": (C.c_int, [P(C.c_double), P(C.c_double), P(Grid), P(C.c_double), P(C.c_double),
+                                        P(C.c_int)]),
         "qssgpu_adjoint_theta": (C.c_int, [P(Options), P(QSSDataArrays), P(Grid), P(C.c_double), P(C.c_double),
                                            C.c_int, C.c_double, C.c_int, P(C.c_double), P(C.c_double)]),
         "qssgpu_forward_theta": (C.c_int, [P(Options), P(QSSDataArrays), P(Grid), P(C.c_double), P(C.c_double),

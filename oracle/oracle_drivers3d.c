@@ -15,6 +15,10 @@
  *   drain_model3d              src/level_set_evolution/drain_model3d.c:49-165
  *   imbibe_model3d             src/level_set_evolution/imbibe_model3d.c:49-161
  *   reinitializeSubcellFix3d   src/reinitialization/reinitialize_top.c:297-377
+ *   qss_reinitialize_mask      src/utilities/qss_general_util.c:261-306
+ *   createMaskUBC, createInitFromMask, makeDiffSteps (logic of the CLIs)
+ *                              src/applications/createMaskUBC.c:76-112,
+ *                              createInitFromMask.c:55-85, makeDiffSteps.c:54-132
  *   trapComponents_mask        src/connectivity/trapComponents.c:156-375
  *   findConnectivity3d         src/connectivity/connectivity.c:48-217
  *   getMainInd_new             src/connectivity/connectivity.c:219-296
@@ -441,6 +445,107 @@ void reinitializeSubcellFix3d(double *data, Grid *g, Options *o)
     }
   }
   free(distance0); free(copy); free(rhs); free(next);
+}
+
+/* ------------------------------------------------------------------ */
+/* mask reinitialisation (qss_general_util.c:261-306): serial, distance0 in
+   scratch1, the initial mask in scratch2, the RHS in lse_rhs, the RK1
+   output in phi_next                                                    */
+void qss_reinitialize_mask(QSS_DataArrays *p, Grid *g, Options *o)
+{
+  double *distance0 = p->scratch1, *copy = p->scratch2;
+  double t_r = 0, dt_r = 0.5 * g->dx[0];
+  arr_copy(copy, p->mask, g->num_gridpts);
+  qss3dcomputedistanceforsubcellfix_(distance0, copy, GBD(g), FBD(g), &g->dx[0], &g->dx[1], &g->dx[2]);
+  while (t_r < o->tmax_r) {
+    qss3dcomputereinitializationeqnrhssubcellfixorder1_(p->lse_rhs, p->mask, GBD(g), copy, distance0,
+                                                        FBD(g), &g->dx[0], &g->dx[1], &g->dx[2]);
+    qss3drk1step_(p->phi_next, GBD(g), p->mask, GBD(g), p->lse_rhs, GBD(g), FBD(g), &dt_r);
+    signedLinearExtrapolationBCqss(p->phi_next, g, 9);
+    arr_copy(p->mask, p->phi_next, g->num_gridpts);
+    t_r = t_r + dt_r;
+  }
+}
+
+/* createMaskUBC.c:76-112 on caller arrays: mask = +-dx from a 255/0 image of
+   the fill box (x fastest), zero ghost layers, then the mask reinitialisation */
+int oracle_create_mask_ubc(const unsigned char *ubc, QSS_DataArrays *p, Grid *g, Options *o)
+{
+  int nx = g->grid_dims_ghostbox[0], nxy = nx * g->grid_dims_ghostbox[1];
+  int fx = g->ihi_fb - g->ilo_fb + 1, fy = g->jhi_fb - g->jlo_fb + 1;
+  arr_fill(p->mask, 0.0, g->num_gridpts);
+  for (int k = g->klo_fb; k <= g->khi_fb; k++)
+    for (int j = g->jlo_fb; j <= g->jhi_fb; j++)
+      for (int i = g->ilo_fb; i <= g->ihi_fb; i++) {
+        int idx = (i - g->ilo_fb) + (j - g->jlo_fb) * fx + (k - g->klo_fb) * fx * fy;
+        int idx_gb = (i - g->ilo_gb) + (j - g->jlo_gb) * nx + (k - g->klo_gb) * nxy;
+        p->mask[idx_gb] = (ubc[idx] == 255) ? o->dx : -o->dx;
+      }
+  qss_reinitialize_mask(p, g, o);
+  return 0;
+}
+
+/* createInitFromMask.c:55-85 (3-D): a sphere around the inlet, then
+   IMPOSE_MASK(phi, mask, phi)                                            */
+int oracle_create_init_from_mask(QSS_DataArrays *p, Grid *g, Options *o)
+{
+  double radius, cx, cy, cz;
+  if (o->center_inlet) {
+    radius = 90 * g->dx[0];
+    cy = 0.5 * (g->x_lo[1] + g->x_hi[1]);
+    cx = 0.5 * (g->x_lo[1] + g->x_hi[1]);
+    cz = 0.5 * (g->x_lo[2] + g->x_hi[2]);
+  } else {
+    radius = 0.7 * (g->x_hi[0] - g->x_lo[0]);
+    cy = 0.5 * (g->x_lo[1] + g->x_hi[1]);
+    cx = (g->x_lo[0]) - radius * 0.7;
+    cz = 0.5 * (g->x_lo[2] + g->x_hi[2]);
+  }
+  createSphere(p->phi, cx, cy, cz, radius, -1, g);
+  arr_max_into(p->phi, p->mask, p->phi, g->num_gridpts);
+  return 0;
+}
+
+/* makeDiffSteps.c:54-132 (3-D) on arrays: diff = max(-a, b - dx/2), then the
+   inlet/outlet slabs, 26-connected labels and the percolation check; when
+   it percolates, connected = diff with the non-wetting voxels outside the
+   main component flipped                                                   */
+void findConnectivity3d(QSS_DataArrays *p, Grid *g);
+int oracle_diff_steps(const double *a, const double *b, Grid *g, double *diff, double *connected,
+                      int *percolates)
+{
+  int n = g->num_gridpts, nx = g->grid_dims_ghostbox[0], nxy = nx * g->grid_dims_ghostbox[1];
+  QSS_DataArrays q;
+  memset(&q, 0, sizeof q);
+  q.phi_bin = (unsigned char *)malloc((size_t)n);
+  q.connectivity = (int *)malloc((size_t)n * sizeof(int));
+  for (int i = 0; i < n; i++) {
+    double m = -a[i];
+    double ph = b[i];
+    ph -= 0.5 * g->dx[0];
+    diff[i] = (m > ph) ? m : ph;
+    q.phi_bin[i] = (diff[i] < 0) ? 1 : 0;
+  }
+  for (int k = g->klo_fb; k <= g->khi_fb; k++)
+    for (int j = g->jlo_fb; j <= g->jhi_fb; j++) {
+      q.phi_bin[(g->ilo_fb - 1) + j * nx + k * nxy] = 1;
+      q.phi_bin[(g->ihi_fb + 1) + j * nx + k * nxy] = 1;
+    }
+  findConnectivity3d(&q, g);
+  int j = 0.5 * (g->jlo_fb + g->jhi_fb), k = 0.5 * (g->klo_fb + g->khi_fb);
+  int inlet = (g->ilo_fb - 1) + j * nx + k * nxy, outlet = (g->ihi_fb + 1) + j * nx + k * nxy;
+  *percolates = q.connectivity[inlet] == q.connectivity[outlet];
+  if (*percolates && connected) {
+    int main_val = q.connectivity[inlet];
+    for (int i = 0; i < n; i++) {
+      double ph = diff[i];
+      if ((q.connectivity[i] != main_val) & (ph <= 0)) ph *= -1;
+      connected[i] = ph;
+    }
+  }
+  free(q.phi_bin);
+  free(q.connectivity);
+  return 0;
 }
 
 /* ------------------------------------------------------------------ */

@@ -87,3 +87,17 @@ def test_model_direct_call(ref, oracle):
     (tr, wr), (to, wo) = _both(ref, oracle, run, threads=3)
     assert tr == to
     assert diff_arrays(wr, wo) == {}
+
+
+def test_reinitialize_mask(ref, oracle):
+    """qss_reinitialize_mask: the mask and its side effects on scratch1,
+    scratch2, lse_rhs and phi_next."""
+    g, v = pack_case(oracle, 18, seed=41)
+
+    def run(lib):
+        w = clone(v)
+        lib.qss_reinitialize_mask(C.byref(w.p), C.byref(g), C.byref(options(lib)))
+        return w
+
+    wr, wo = _both(ref, oracle, run)
+    assert diff_arrays(wr, wo) == {}
