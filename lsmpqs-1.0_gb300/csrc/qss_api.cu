@@ -409,7 +409,13 @@ double constCurvModel3d(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out) {
     v.inner_steps = v.outer_iters = 0;
     reset_phases(v);
     upload_for_const_curv(v, p, o, true);
+    if (o->check_connectivity)
+      start_prefault(v, p, {H_PHI_NEXT, H_PHI_PREV, H_LSE_RHS, H_SCRATCH1, H_SCRATCH2, H_MASK_W, H_MASK_NW,
+                            H_CONN, H_BIN});
+    else
+      start_prefault(v, p, {H_PHI_NEXT, H_PHI_PREV, H_LSE_RHS, H_SCRATCH1, H_SCRATCH2});
   }
+  PrefaultGuard pg{v};
   double t = dev_const_curv(v, true, o, p, g, fp_out, 0.0);
   if (scope.outermost()) download_dirty(v, p);
   return t;
@@ -425,7 +431,13 @@ double constCurvModel3dNoVar(Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_ou
     v.inner_steps = v.outer_iters = 0;
     reset_phases(v);
     upload_for_const_curv(v, p, o, false);
+    if (o->check_connectivity)
+      start_prefault(v, p, {H_PHI_NEXT, H_PHI_PREV, H_LSE_RHS, H_SCRATCH1, H_SCRATCH2, H_MASK_W, H_MASK_NW,
+                            H_CONN, H_BIN});
+    else
+      start_prefault(v, p, {H_PHI_NEXT, H_PHI_PREV, H_LSE_RHS, H_SCRATCH1, H_SCRATCH2});
   }
+  PrefaultGuard pg{v};
   double t = dev_const_curv(v, false, o, p, g, fp_out, a);
   if (scope.outermost()) download_dirty(v, p);
   return t;

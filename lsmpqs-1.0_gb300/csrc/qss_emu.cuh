@@ -389,6 +389,32 @@ QSS_EMU_HD double scale2(double x, int k) {
 }
 
 // ---------------------------------------------------------------------------
+// sign flip and absolute value on the integer pipes.  Written as plain bit
+// operations the compiler recognises them as FP64 negation / fabs and may
+// issue them as FP64-pipe additions; the PTX logic op on the high word keeps
+// them integer instructions.
+
+QSS_EMU_HD double neg(double x) {
+#ifdef __CUDA_ARCH__
+  int hi = __double2hiint(x);
+  asm("xor.b32 %0, %0, 0x80000000;" : "+r"(hi));
+  return __hiloint2double(hi, __double2loint(x));
+#else
+  return from_bits(bits(x) ^ kSign);
+#endif
+}
+
+QSS_EMU_HD double abs(double x) {
+#ifdef __CUDA_ARCH__
+  int hi = __double2hiint(x);
+  asm("and.b32 %0, %0, 0x7fffffff;" : "+r"(hi));
+  return __hiloint2double(hi, __double2loint(x));
+#else
+  return from_bits(bits(x) & kAbs);
+#endif
+}
+
+// ---------------------------------------------------------------------------
 // comparisons with IEEE semantics (false for NaN operands, -0 == +0)
 
 QSS_EMU_HD bool isnan_bits(uint64_t b) { return (b & kAbs) > 0x7ff0000000000000ull; }

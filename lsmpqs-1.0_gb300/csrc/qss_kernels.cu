@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <utility>
 #include <vector>
+#include "qss_emu.cuh"
 #include "qss_kernels.cuh"
 
 namespace qss {
@@ -409,15 +410,74 @@ __device__ __forceinline__ double reinit_rhs_at(const double* __restrict__ phi, 
   return d0 - sgn * fabs(cc) / max_dx;
 }
 
+// The same right-hand side with the sign tests, maxima, absolute values, the
+// square root and the division on the integer pipes (qss_emu: IEEE results,
+// bit for bit), leaving ~20 FP64 instructions per voxel; at EMU >= 2 the six
+// scalings of the one-sided differences move there too.  Every branch
+// computes exactly the native version's value:
+//   dmax(-g, 0) = (g < 0 ? -g : +0) and dmax(g, 0) = (g > 0 ? g : +0) (only
+//   their squares are used, so the sign of a zero does not matter);
+//   sgn * s for sgn = +-1 is a sign flip; sgn = 0 keeps the native product.
+template <int EMU>
+__device__ __forceinline__ double reinit_rhs_e(const double* __restrict__ phi, const double* __restrict__ phi0,
+                                               const double* __restrict__ distance0, const Box& b, int64_t c,
+                                               const Inv& inv, double max_dx, uint64_t far_bits) {
+  using namespace qss_emu;
+  const uint64_t tol_bits = bits(1.e-5);
+  const int64_t sy = b.sy(), sz = b.sz();
+  auto scale = [](double d, double f) -> double { return EMU >= 2 ? qss_emu::mul(d, f) : d * f; };
+  const double cc = __ldg(phi + c);
+  const double p0 = phi0[c];
+  const uint64_t ap0 = bits(p0) & kAbs;
+  const bool sgn_nz = ap0 > tol_bits && ap0 <= 0x7ff0000000000000ull;  // fabs(p0) > 1e-5
+  const bool sgn_neg = (int64_t)bits(p0) < 0;
+  const double sgn = sgn_nz ? (sgn_neg ? -1.0 : 1.0) : 0.0;
+  const double d0 = distance0[c];
+  if (bits(d0) == far_bits) {
+    const bool pos = gt0(cc);
+    double gs[3];
+    const int64_t st[3] = {1, sy, sz};
+    const double iv[3] = {inv.x, inv.y, inv.z};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double gp = scale(__ldg(phi + c + st[d]) - cc, iv[d]);
+      const double gm = scale(cc - __ldg(phi + c - st[d]), iv[d]);
+      double a_, b_;
+      if (pos) {
+        a_ = lt0(gp) ? qss_emu::neg(gp) : 0.0;
+        b_ = gt0(gm) ? gm : 0.0;
+      } else {
+        a_ = gt0(gp) ? gp : 0.0;
+        b_ = lt0(gm) ? qss_emu::neg(gm) : 0.0;
+      }
+      gs[d] = max_nonneg(a_, b_);
+    }
+    const uint64_t acc = bits(cc) & kAbs;
+    if (acc > tol_bits && acc <= 0x7ff0000000000000ull) {  // fabs(cc) > 1e-5
+      const double ngps = gs[0] * gs[0] + gs[1] * gs[1] + gs[2] * gs[2];
+      const double s = qss_emu::sqrt(ngps);
+      if (!sgn_nz) return sgn - sgn * s;
+      return sgn - (sgn_neg ? qss_emu::neg(s) : s);
+    }
+    return 0.0;
+  }
+  // d0 - sgn * fabs(cc) / max_dx
+  const double acc = qss_emu::abs(cc);
+  const double t = sgn_nz ? (sgn_neg ? qss_emu::neg(acc) : acc) : sgn * acc;
+  return d0 - qss_emu::div(t, max_dx);
+}
+
+template <int EMU>
 __global__ void k_reinit_step(Box b, const double* __restrict__ data, const double* __restrict__ phi0,
                               const double* __restrict__ distance0, double* __restrict__ next, double dt_r,
-                              Inv inv, double max_dx, int rhs_only) {
+                              Inv inv, double max_dx, int rhs_only, uint64_t far_bits) {
   const int i = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = b.jlo + blockIdx.y * blockDim.y + threadIdx.y;
   const int k = b.klo + blockIdx.z * blockDim.z + threadIdx.z;
   if (i > b.ihi || j > b.jhi || k > b.khi) return;
   const int64_t c = b.idx(i, j, k);
-  const double r = reinit_rhs_at(data, phi0, distance0, b, c, inv, max_dx);
+  const double r = EMU == 0 ? reinit_rhs_at(data, phi0, distance0, b, c, inv, max_dx)
+                            : reinit_rhs_e<EMU>(data, phi0, distance0, b, c, inv, max_dx, far_bits);
   next[c] = rhs_only ? r : data[c] + dt_r * r;
 }
 
@@ -860,18 +920,30 @@ void launch_distance0(cudaStream_t s, const Box& b, const double* phi0, double* 
   k_distance0<<<fb_grid(b, kBlk3), kBlk3, 0, s>>>(b, phi0, distance0, dx, dy, dz);
 }
 
+static void reinit_launch(cudaStream_t s, const Box& b, const double* data, const double* phi0,
+                          const double* distance0, double* out, double dt_r, double dx, double dy, double dz,
+                          int rhs_only) {
+  const double max_dx = (dx > dy ? dx : dy) > dz ? (dx > dy ? dx : dy) : dz;
+  const Inv inv{1.0 / dx, 1.0 / dy, 1.0 / dz};
+  const uint64_t far_bits = qss_emu::bits(-1000.0 * max_dx);  // distance0 of voxels away from the interface
+  const int lvl = emu_level();
+  const dim3 grid = fb_grid(b, kBlk3);
+  if (lvl >= 2)
+    k_reinit_step<2><<<grid, kBlk3, 0, s>>>(b, data, phi0, distance0, out, dt_r, inv, max_dx, rhs_only, far_bits);
+  else if (lvl == 1)
+    k_reinit_step<1><<<grid, kBlk3, 0, s>>>(b, data, phi0, distance0, out, dt_r, inv, max_dx, rhs_only, far_bits);
+  else
+    k_reinit_step<0><<<grid, kBlk3, 0, s>>>(b, data, phi0, distance0, out, dt_r, inv, max_dx, rhs_only, far_bits);
+}
+
 void launch_reinit_step(cudaStream_t s, const Box& b, const double* data, const double* phi0,
                         const double* distance0, double* next, double dt_r, double dx, double dy, double dz) {
-  const double max_dx = (dx > dy ? dx : dy) > dz ? (dx > dy ? dx : dy) : dz;
-  k_reinit_step<<<fb_grid(b, kBlk3), kBlk3, 0, s>>>(b, data, phi0, distance0, next, dt_r,
-                                                     Inv{1.0 / dx, 1.0 / dy, 1.0 / dz}, max_dx, 0);
+  reinit_launch(s, b, data, phi0, distance0, next, dt_r, dx, dy, dz, 0);
 }
 
 void launch_reinit_rhs(cudaStream_t s, const Box& b, const double* data, const double* phi0,
                        const double* distance0, double* rhs, double dx, double dy, double dz) {
-  const double max_dx = (dx > dy ? dx : dy) > dz ? (dx > dy ? dx : dy) : dz;
-  k_reinit_step<<<fb_grid(b, kBlk3), kBlk3, 0, s>>>(b, data, phi0, distance0, rhs, 0.0,
-                                                     Inv{1.0 / dx, 1.0 / dy, 1.0 / dz}, max_dx, 1);
+  reinit_launch(s, b, data, phi0, distance0, rhs, 0.0, dx, dy, dz, 1);
 }
 
 void launch_central_grad(cudaStream_t s, const Box& b, const double* f, double* fx, double* fy, double* fz,

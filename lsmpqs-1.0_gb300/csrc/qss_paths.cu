@@ -84,7 +84,14 @@ void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out
   if (outermost) {
     upload(v, p, H_PHI);
     upload(v, p, H_MASK);
+    if (o->theta > 0 || o->use_var_theta)
+      start_prefault(v, p, {H_PHI_NEXT, H_PHI_PREV, H_PHI_EXTRA, H_MASK_W, H_MASK_NW, H_MASK_DISCONN, H_MASK_X,
+                            H_MASK_Y, H_MASK_Z, H_CONN, H_BIN, H_VEL_N, H_BCOEF, H_VX, H_VY, H_VZ});
+    else
+      start_prefault(v, p, {H_PHI_NEXT, H_PHI_PREV, H_PHI_EXTRA, H_MASK_W, H_MASK_NW, H_MASK_DISCONN, H_MASK_X,
+                            H_MASK_Y, H_MASK_Z, H_CONN, H_BIN});
   }
+  PrefaultGuard pg{v};
   char fname[256];
   int dims[3];
   double a0 = o->a;

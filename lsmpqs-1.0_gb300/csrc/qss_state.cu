@@ -7,6 +7,9 @@
 #include <mutex>
 #include <unordered_map>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "qss_state.h"
 
 namespace qss {
@@ -24,6 +27,13 @@ int g_slabs_override = 0;
 int g_weno_split = -1;  // -1: from the environment
 int g_emu_level = -1;   // -1: from the environment
 }  // namespace
+
+// MADV_POPULATE_WRITE (Linux 5.14); older headers lack the name
+#ifdef MADV_POPULATE_WRITE
+constexpr int kMadvPopulateWrite = MADV_POPULATE_WRITE;
+#else
+constexpr int kMadvPopulateWrite = 23;
+#endif
 
 static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -308,8 +318,53 @@ void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which) {
   QSS_CK(cudaMemcpyAsync(d, h, (size_t)v.n * elem_size(which), cudaMemcpyHostToDevice, v.stream));
 }
 
+void HostPrefault::start(const std::vector<std::pair<void*, size_t>>& ranges) {
+  join();
+  if (ranges.empty()) return;
+  const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
+  const size_t nw = ranges.size() < 2 ? ranges.size() : 2;
+  for (size_t w = 0; w < nw; w++) {
+    std::vector<std::pair<void*, size_t>> mine;
+    for (size_t r = w; r < ranges.size(); r += nw) mine.push_back(ranges[r]);
+    workers.emplace_back([mine, page] {
+      for (const auto& r : mine) {
+        const uintptr_t lo = (uintptr_t)r.first & ~(page - 1);
+        const uintptr_t hi = ((uintptr_t)r.first + r.second + page - 1) & ~(page - 1);
+        // failure (an older kernel, a mapping that refuses) leaves the pages as they are
+        (void)madvise((void*)lo, hi - lo, kMadvPopulateWrite);
+      }
+    });
+  }
+}
+
+void HostPrefault::join() {
+  for (auto& t : workers)
+    if (t.joinable()) t.join();
+  workers.clear();
+}
+
+void start_prefault(DevVolume& v, const QSS_DataArrays* p, std::initializer_list<HostArray> which) {
+  std::vector<std::pair<void*, size_t>> ranges;
+  for (HostArray a : which) {
+    void* h = host_ptr(p, a);
+    if (usable(h)) ranges.emplace_back(h, (size_t)v.n * elem_size(a));
+  }
+  v.prefault.start(ranges);
+}
+
 void download_dirty(DevVolume& v, QSS_DataArrays* p) {
   PhaseTimer pt(v, PH_DOWNLOAD);
+  v.prefault.join();
+  // arrays the reference leaves zero: cleared on host threads, one per array,
+  // while the copies run
+  struct Joiner {
+    std::vector<std::thread> t;
+    ~Joiner() {
+      for (auto& x : t)
+        if (x.joinable()) x.join();
+    }
+  } clear;
+  bool synced = false;
   for (int a = 0; a < H_COUNT; a++) {
     HostArray w = (HostArray)a;
     void* h = host_ptr(p, w);
@@ -318,8 +373,10 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
       continue;
     }
     if (v.zero_on_return[a]) {
-      QSS_CK(cudaStreamSynchronize(v.stream));
-      memset(h, 0, (size_t)v.n * elem_size(w));
+      if (!synced) QSS_CK(cudaStreamSynchronize(v.stream));
+      synced = true;
+      const size_t bytes = (size_t)v.n * elem_size(w);
+      clear.t.emplace_back([h, bytes] { memset(h, 0, bytes); });
     } else if (v.dirty[a]) {
       void* d = dev_ptr(v, w);
       if (!d) continue;
@@ -340,6 +397,7 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
     }
     v.dirty[a] = v.zero_on_return[a] = false;
   }
+  for (auto& t : clear.t) t.join();
   QSS_CK(cudaStreamSynchronize(v.stream));
 }
 

@@ -5,6 +5,9 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <initializer_list>
+#include <thread>
+#include <vector>
 
 #include "../../include/lsmpqs_gpu.h"
 #include "../../include/lsmpqs_types.h"
@@ -51,6 +54,20 @@ enum HostArray {
   H_MASK_DISCONN, H_COUNT
 };
 
+// Background population of the host pages a call will copy results into.
+// A device-to-host copy into anonymous pages that were never written runs at
+// the speed of the page faults (~25 GB/s measured on the Grace host, ~190
+// GB/s into resident pages), so the outermost call asks the kernel to make
+// those pages resident and writable (madvise MADV_POPULATE_WRITE, which
+// leaves their contents unchanged) on host threads while the device
+// computes.  Kernels without that advice leave the pages as they are.
+struct HostPrefault {
+  std::vector<std::thread> workers;
+  void start(const std::vector<std::pair<void*, size_t>>& ranges);
+  void join();
+  ~HostPrefault() { join(); }
+};
+
 struct DevVolume {
   const QSS_DataArrays* key = nullptr;
   Box box{};
@@ -88,6 +105,7 @@ struct DevVolume {
   // host wall time per phase of the last top-level call (PhaseTimer)
   double phase_s[8] = {};
   int phase_open = -1;
+  HostPrefault prefault;
 };
 
 DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g);
@@ -96,6 +114,14 @@ void release_volume(const QSS_DataArrays* p);
 // host <-> device copies of one array of the struct
 void upload(DevVolume& v, const QSS_DataArrays* p, HostArray which);
 void download_dirty(DevVolume& v, QSS_DataArrays* p);
+// populates in the background the host pages of the given arrays of p (the
+// ones the call will write); download_dirty waits for it
+void start_prefault(DevVolume& v, const QSS_DataArrays* p, std::initializer_list<HostArray> which);
+// waits for the background population when the call leaves early (error)
+struct PrefaultGuard {
+  DevVolume& v;
+  ~PrefaultGuard() { v.prefault.join(); }
+};
 
 int num_slabs_for(const Grid* g);
 // throws unless g is a 3-D grid the device path supports (>= 3 ghost layers)

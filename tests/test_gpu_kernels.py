@@ -177,20 +177,36 @@ def test_coefficients(gpu, oracle):
         assert np.array_equal(a, b)
 
 
-def test_reinit_kernels(gpu, oracle):
+@pytest.mark.parametrize("emu", [0, 1, 2])
+def test_reinit_kernels(gpu, oracle, emu):
+    """Distance function and reinitialisation RHS, with the RHS's tests, square
+    root and division natively (0) or on the integer pipes (1, 2); phi0 holds
+    values inside the +-1e-5 band (sign 0) and signed zeros, phi holds flat
+    patches (zero one-sided differences)."""
     g, v = pack_case(oracle, N, seed=5)
+    rng = np.random.default_rng(55)
     phi0 = v["phi"].copy()
+    sel = rng.random(phi0.shape) < 0.05
+    phi0[sel] = rng.choice([0.0, -0.0, 5e-6, -5e-6, 1e-5, -1e-5], sel.sum())
     phi = phi0 + 0.01 * np.sin(np.arange(phi0.size).reshape(phi0.shape))
+    flat = rng.random(phi.shape) < 0.1
+    phi[flat] = 0.02
+    phi[rng.random(phi.shape) < 0.02] = rng.choice([0.0, -0.0, 1e-5, -1e-5, 3e-6])
     res = []
-    for lib in (gpu, oracle):
-        d0 = np.zeros(v.shape)
-        lib.qss3dcomputedistanceforsubcellfix_(Q.dptr(d0), Q.dptr(phi0), *Q.gb_args(g), *Q.fb_args(g),
-                                               Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]))
-        rhs = np.zeros(v.shape)
-        lib.qss3dcomputereinitializationeqnrhssubcellfixorder1_(
-            Q.dptr(rhs), Q.dptr(phi), *Q.gb_args(g), Q.dptr(phi0), Q.dptr(d0), *Q.fb_args(g), Q.dref(g.dx[0]),
-            Q.dref(g.dx[1]), Q.dref(g.dx[2]))
-        res.append((d0, rhs))
+    prev = gpu.qssgpu_set_emu_level(emu)
+    try:
+        libs = (gpu, oracle)
+        for lib in libs:
+            d0 = np.zeros(v.shape)
+            lib.qss3dcomputedistanceforsubcellfix_(Q.dptr(d0), Q.dptr(phi0), *Q.gb_args(g), *Q.fb_args(g),
+                                                   Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]))
+            rhs = np.zeros(v.shape)
+            lib.qss3dcomputereinitializationeqnrhssubcellfixorder1_(
+                Q.dptr(rhs), Q.dptr(phi), *Q.gb_args(g), Q.dptr(phi0), Q.dptr(d0), *Q.fb_args(g),
+                Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]))
+            res.append((d0, rhs))
+    finally:
+        gpu.qssgpu_set_emu_level(prev)
     Q.check(gpu)
     assert np.array_equal(res[0][0], res[1][0])
     assert np.array_equal(res[0][1], res[1][1])

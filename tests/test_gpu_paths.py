@@ -63,14 +63,19 @@ def test_trap_components(gpu, oracle, center):
     assert (b["mask_w"] > 0).any() or (b["mask_nw"] > 0).any()
 
 
-def test_reinitialize(gpu, oracle):
+@pytest.mark.parametrize("emu", [0, 1, 2])
+def test_reinitialize(gpu, oracle, emu):
     g, v = pack_case(oracle, 24, seed=3)
     o = options(oracle)
     outs = []
-    for lib in (gpu, oracle):
-        a = v["mask"].copy()
-        lib.reinitializeSubcellFix3d(Q.dptr(a), C.byref(g), C.byref(o))
-        outs.append(a)
+    prev = gpu.qssgpu_set_emu_level(emu)
+    try:
+        for lib in (gpu, oracle):
+            a = v["mask"].copy()
+            lib.reinitializeSubcellFix3d(Q.dptr(a), C.byref(g), C.byref(o))
+            outs.append(a)
+    finally:
+        gpu.qssgpu_set_emu_level(prev)
     Q.check(gpu)
     assert np.array_equal(outs[0], outs[1])
 
