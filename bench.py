@@ -180,6 +180,11 @@ KERNEL_NAME = {0: "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
                3: "k_weno_axis<2> (WENO5 z-pass, shared sub-expressions)",
                4: "k_weno_combine (Godunov + advection + curvature + TVD-RK)"}
 N_KINDS = 5
+# DRAM bytes per fill-box voxel of one launch of each stage kernel, measured at
+# 512^3 with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass):
+# x pass 7.74 GB, y pass 3.40 GB, z pass 3.37 GB, combine 14.22 GB for 134.2 M
+# voxels; the fused kernel was not captured
+TRAFFIC_BYTES_PER_VOXEL = {1: 57.7, 2: 25.3, 3: 25.1, 4: 105.9}
 # algorithmic HBM bytes per voxel-step (each array touched once per stage):
 # stage 1 phi + 5 coefficients -> phi1, stage 2 phi1 + phi + 5 coeff -> phi2,
 # stage 3 phi2 + phi + 5 coeff + 3 masks -> phi1, phi
@@ -251,7 +256,10 @@ def gpu_arm(args, dist: Dist):
     stage_total_ms = out[3] / args.steps
     achieved_gbs = BYTES_PER_VOXEL_STEP * nvox / (stage_total_ms / 1e3) / 1e9 if stage_total_ms > 0 else 0.0
     roofline = {"bound": "fp64", "achieved": round(achieved_tf, 4), "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": round(achieved_tf / fp64_peak, 4) if fp64_peak else None, "traffic": args.traffic,
+                "frac": round(achieved_tf / fp64_peak, 4) if fp64_peak else None,
+                "traffic": args.traffic if args.traffic is not None else (
+                    round(TRAFFIC_BYTES_PER_VOXEL[top] * nvox) if top in TRAFFIC_BYTES_PER_VOXEL else None),
+                "traffic_unit": "bytes per launch (ncu at 512^3, scaled per voxel to this size)",
                 "kernel": KERNEL_NAME[top], "flop_per_voxel": FLOP_PER_VOXEL[top],
                 "launch_ms": round(top_ms, 4), "kernels": kinds,
                 "peak_source": peak_src,
@@ -531,7 +539,7 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-ckpt", type=int, default=20)
     ap.add_argument("--traffic", type=float, default=None,
-                    help="DRAM bytes per stage launch from an ncu capture (optional)")
+                    help="DRAM bytes per launch of the roofline kernel (overrides the measured table)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, _, local = dist_info()
