@@ -253,6 +253,16 @@ int qssgpu_create_init_from_mask(QSS_DataArrays *p, Grid *g, Options *o);
    arrays. */
 int qssgpu_diff_steps(const double *step_a, const double *step_b, Grid *g, double *diff, double *connected,
                       int *percolates);
+/* makeRaw's phase images (src/applications/makeRaw.c:52-135): 1 where the
+   selected level set is negative, else 0 (IMPOSE_UCHAR), for phase 'm' the
+   mask, 'n' phi (non-wetting), 'w' max(mask, -phi) (wetting); bin_full gets
+   the ghost-box image, bin_fb the fill box packed i fastest (copyDataFB);
+   either may be NULL, phi / mask only where the phase reads them.  The
+   reference writes its `_fb` images of phases n and w with the ghost-box
+   byte count from a fill-box buffer (an over-read); here the fill-box image
+   has exactly the fill-box bytes. */
+int qssgpu_phase_uchar(const double *phi, const double *mask, Grid *g, char phase, unsigned char *bin_full,
+                       unsigned char *bin_fb);
 /* Adjoint mode (no reference counterpart).  Forward model: nsteps TVD-RK3
    steps of the variable-coefficient WENO5 update of constCurvModel3d with a
    fixed time step dt (no connectivity, reinitialisation or CFL), starting from

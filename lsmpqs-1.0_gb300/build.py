@@ -5,7 +5,11 @@
 Every CUDA translation unit is compiled for sm_103a only, with --fmad=false:
 the kernels restate the reference's FP64 arithmetic operation by operation,
 and a fused multiply-add would round differently.  Host code is compiled
-without floating-point contraction for the same reason.  Translation units
+without floating-point contraction for the same reason.  The exception is
+the adjoint's reverse kernels (qss_adjoint.cu): a gradient has no reference
+bit pattern to match, so they may fuse multiply-adds (fewer FP64
+instructions on the pipe that bounds them); the forward model they
+differentiate runs in the other, uncontracted translation units.  Translation units
 are compiled in parallel; the shared library links the CUDA runtime
 statically so it only needs the driver at run time.
 """
@@ -42,9 +46,16 @@ def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
+# translation units allowed to contract a * b + c into one FMA
+FMAD_UNITS = {"qss_adjoint.cu"}
+
+
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-    cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+    flags = NVCC_FLAGS
+    if os.path.basename(src) in FMAD_UNITS:
+        flags = ["--fmad=true" if f == "--fmad=false" else f for f in NVCC_FLAGS]
+    cmd = [nvcc()] + flags + ["-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "c++", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math", "-c", src, "-o", obj]

@@ -13,19 +13,27 @@
 // The forward runs the production kernels (split WENO5 passes + combine);
 // the time step is an input, so no gradient flows through the CFL estimate.
 //
-// Backward (reverse mode by hand, FP64): for each stage, one thread per
-// fill-box voxel recomputes the stage's RHS at that voxel and its partials
-// with respect to the 31 stencil values it reads (axis offsets +-1..3, the 12
-// edge neighbours of the mixed derivatives, the centre) and to vel_n, and
-// stores partial x adjoint weight per offset; a gather kernel then forms
-// each point's adjoint as the sum over the voxels whose stencil contains it,
-// in a fixed order (deterministic, no atomics).  Voxels whose normal term is
-// carried from an earlier voxel (|vel_n| < 1e-5, 3d.f:459-486) add their
-// (rare) contributions to that voxel's stencil by atomics.  The boundary
-// extrapolation is reversed face by face (z, then y, then x), the
-// imposition passes the adjoint where the stage value was kept.  Steps are
+// Backward (reverse mode by hand, FP64), per stage: k_adj_point takes each
+// fill-box voxel's adjoint weight through the Godunov normal term, the upwind
+// advection and the curvature, giving the adjoints of its six one-sided
+// WENO5 derivatives and the partials of the curvature with respect to its
+// central differences; k_adj_axis (one per axis) takes the derivative
+// adjoints back to phi line by line, one WENO5 face window at a time for the
+// minus derivative of one voxel and the plus derivative of its neighbour
+// together (they share the window's smoothness indicators); k_adj_curv
+// gathers the curvature partials.  Every point's adjoint is summed in a fixed
+// order (deterministic); voxels whose normal term is carried from an earlier
+// voxel (|vel_n| < 1e-5, 3d.f:459-486) add their (rare) contributions to
+// that voxel's derivative adjoints by atomics.  The boundary extrapolation
+// is reversed face by face (z, then y, then x), the imposition passes the
+// adjoint where the stage value was kept.  Steps are
 // recomputed from checkpoints every `ckpt` steps, storing the stage states
 // of one segment at a time.
+//
+// This translation unit is compiled with FMA contraction: the reverse
+// arithmetic has no reference bit pattern to reproduce (the forward steps run
+// the uncontracted production kernels), and fused multiply-adds cut the FP64
+// instructions of the reverse kernel, which is bound by the FP64 pipe.
 #include <vector>
 
 #include "qss_emu.cuh"
@@ -35,140 +43,8 @@ namespace qss {
 
 namespace {
 
-constexpr int kOff = 31;  // stencil offsets of one voxel's RHS
-
-// offset o -> (di, dj, dk):  0 centre; 1..18 axis d = (o-1)/6, distance
-// -3,-2,-1,+1,+2,+3; 19..22 xy (+1,+1)(-1,-1)(-1,+1)(+1,-1); 23..26 xz; 27..30 yz
-__host__ __device__ __forceinline__ void offset_of(int o, int& di, int& dj, int& dk) {
-  di = dj = dk = 0;
-  if (o == 0) return;
-  if (o <= 18) {
-    const int d = (o - 1) / 6, r = (o - 1) % 6;
-    const int k = r < 3 ? r - 3 : r - 2;
-    if (d == 0) di = k;
-    else if (d == 1) dj = k;
-    else dk = k;
-    return;
-  }
-  const int e = (o - 19) / 4, r = (o - 19) % 4;
-  const int a = (r == 0) ? 1 : (r == 1 ? -1 : (r == 2 ? -1 : 1));
-  const int c = (r == 0) ? 1 : (r == 1 ? -1 : (r == 2 ? 1 : -1));
-  if (e == 0) {
-    di = a;
-    dj = c;
-  } else if (e == 1) {
-    di = a;
-    dk = c;
-  } else {
-    dj = a;
-    dk = c;
-  }
-}
-
-__device__ __forceinline__ int axis_off(int d, int k) { return 1 + 6 * d + (k < 0 ? k + 3 : k + 2); }
-
 constexpr double kC13 = 1.0 / 3.0, kC76 = 7.0 / 6.0, kC116 = 11.0 / 6.0, kC16 = 1.0 / 6.0, kC56 = 5.0 / 6.0;
-constexpr double k1312 = 13.0 / 12.0;
-
-// adjoint of one WENO5 side (3d.f:1999-2014): accumulates into vb[0..4] the
-// partials of the side's value times gbar (four divisions, on the integer
-// pipes)
-__device__ __forceinline__ void weno_side_bwd(const double v[5], double gbar, double vb[5]) {
-  // eps: the reference's chain of MAX keeps the later operand on ties; the
-  // squares are non-negative, so their bit patterns order like the values
-  // (integer compares, static indices only: no local memory)
-  long long mb = (long long)qss_emu::bits(v[0] * v[0]);
-  int im = 0;
-  double vim = v[0];
-#pragma unroll
-  for (int i = 1; i < 5; i++) {
-    const long long qb = (long long)qss_emu::bits(v[i] * v[i]);
-    if (!(mb > qb)) {
-      mb = qb;
-      im = i;
-      vim = v[i];
-    }
-  }
-  const double eps = 1e-6 * qss_emu::from_bits((unsigned long long)mb) + 1.0e-35;
-  const double p1 = kC13 * v[0] - kC76 * v[1] + kC116 * v[2];
-  const double p2 = -(kC16 * v[1]) + kC56 * v[2] + kC13 * v[3];
-  const double p3 = kC13 * v[2] + kC56 * v[3] - kC16 * v[4];
-  const double t1a = v[0] - 2.0 * v[1] + v[2], t1b = v[0] - 4.0 * v[1] + 3.0 * v[2];
-  const double t2a = v[1] - 2.0 * v[2] + v[3], t2b = v[1] - v[3];
-  const double t3a = v[2] - 2.0 * v[3] + v[4], t3b = 3.0 * v[2] - 4.0 * v[3] + v[4];
-  const double S1 = k1312 * (t1a * t1a) + 0.25 * (t1b * t1b);
-  const double S2 = k1312 * (t2a * t2a) + 0.25 * (t2b * t2b);
-  const double S3 = k1312 * (t3a * t3a) + 0.25 * (t3b * t3b);
-  const double iT1 = qss_emu::div(1.0, S1 + eps), iT2 = qss_emu::div(1.0, S2 + eps),
-               iT3 = qss_emu::div(1.0, S3 + eps);
-  const double a1 = 0.1 * iT1 * iT1, a2 = 0.6 * iT2 * iT2, a3 = 0.3 * iT3 * iT3;
-  const double iA = qss_emu::div(1.0, a1 + a2 + a3);
-  const double w1 = a1 * iA, w2 = a2 * iA, w3 = a3 * iA;
-  // reverse
-  const double pb1 = gbar * w1, pb2 = gbar * w2, pb3 = gbar * w3;
-  const double wb1 = gbar * p1, wb2 = gbar * p2, wb3 = gbar * p3;
-  const double sw = wb1 * w1 + wb2 * w2 + wb3 * w3;
-  const double Tb1 = -2.0 * (wb1 - sw) * iA * a1 * iT1, Tb2 = -2.0 * (wb2 - sw) * iA * a2 * iT2,
-               Tb3 = -2.0 * (wb3 - sw) * iA * a3 * iT3;
-  const double epsb = Tb1 + Tb2 + Tb3;
-  {
-    // vb[im] += d eps / d v[im] * epsb, with the index resolved by selects
-    double t = vb[0];
-#pragma unroll
-    for (int i = 1; i < 5; i++) t = (im == i) ? vb[i] : t;
-    t += epsb * 2e-6 * vim;
-#pragma unroll
-    for (int i = 0; i < 5; i++) vb[i] = (im == i) ? t : vb[i];
-  }
-  const double t1ab = Tb1 * 2.0 * k1312 * t1a, t1bb = Tb1 * 0.5 * t1b;
-  vb[0] += t1ab + t1bb;
-  vb[1] += -2.0 * t1ab - 4.0 * t1bb;
-  vb[2] += t1ab + 3.0 * t1bb;
-  const double t2ab = Tb2 * 2.0 * k1312 * t2a, t2bb = Tb2 * 0.5 * t2b;
-  vb[1] += t2ab + t2bb;
-  vb[2] += -2.0 * t2ab;
-  vb[3] += t2ab - t2bb;
-  const double t3ab = Tb3 * 2.0 * k1312 * t3a, t3bb = Tb3 * 0.5 * t3b;
-  vb[2] += t3ab + 3.0 * t3bb;
-  vb[3] += -2.0 * t3ab - 4.0 * t3bb;
-  vb[4] += t3ab + t3bb;
-  vb[0] += kC13 * pb1;
-  vb[1] += -kC76 * pb1 - kC16 * pb2;
-  vb[2] += kC116 * pb1 + kC56 * pb2 + kC13 * pb3;
-  vb[3] += kC13 * pb2 + kC56 * pb3;
-  vb[4] += -kC16 * pb3;
-}
-
-// adjoint of the WENO5 plus/minus derivatives along one axis: P[0..6] =
-// phi(q-3..q+3), output adjoints (pb, mb), accumulated into Pb[0..6]
-__device__ __forceinline__ void weno_axis_bwd(const double P[7], double inv, double pb, double mb, double Pb[7]) {
-  double F[6];  // faces q-2 .. q+3: F[m] = (P[m+1] - P[m]) inv
-#pragma unroll
-  for (int m = 0; m < 6; m++) F[m] = (P[m + 1] - P[m]) * inv;
-  double Fb[6] = {0, 0, 0, 0, 0, 0};
-  if (pb != 0.0) {
-    const double v[5] = {F[5], F[4], F[3], F[2], F[1]};  // plus: faces i+3 .. i-1
-    double vb[5] = {0, 0, 0, 0, 0};
-    weno_side_bwd(v, pb, vb);
-    Fb[5] += vb[0];
-    Fb[4] += vb[1];
-    Fb[3] += vb[2];
-    Fb[2] += vb[3];
-    Fb[1] += vb[4];
-  }
-  if (mb != 0.0) {
-    const double v[5] = {F[0], F[1], F[2], F[3], F[4]};  // minus: faces i-2 .. i+2
-    double vb[5] = {0, 0, 0, 0, 0};
-    weno_side_bwd(v, mb, vb);
-#pragma unroll
-    for (int m = 0; m < 5; m++) Fb[m] += vb[m];
-  }
-#pragma unroll
-  for (int m = 0; m < 6; m++) {
-    Pb[m + 1] += Fb[m] * inv;
-    Pb[m] -= Fb[m] * inv;
-  }
-}
+constexpr double k1312 = 13.0 / 12.0, k136 = 13.0 / 6.0;
 
 // Godunov term of WENO5 (3d.f:2245-2276) and its partials: dtn/d(pp, pm), dtn/dvel
 __device__ __forceinline__ double godunov_bwd(double vel, const double pp[3], const double pm[3], double ppb[3],
@@ -201,185 +77,379 @@ __device__ __forceinline__ double godunov_bwd(double vel, const double pp[3], co
   return vel * norm;
 }
 
-struct AdjRhsArgs {
+struct AdjPointArgs {
   Box b;
   const double* phi;     // stage input, ghosts valid
   const double* dp[3];   // its WENO5 plus/minus derivatives (production axis passes)
   const double* dm[3];
-  const double* wgt;     // adjoint weight of the voxel's RHS (fill box)
+  const double* lam_in;  // adjoint of the stage output; weight of the RHS = coef_l * lam_in (fill box)
+  double coef_l;
   const double* vel_n;
   const double* bcoef;
   const double* vx;
   const double* vy;
   const double* vz;
   const int* nsrc;
-  double inv[3];
-  double fac[3];
-  double* contrib;       // kOff arrays of npts: contrib[o * npts + q]
+  double fac[3];         // 1 / (2 dx) per axis
+  double f2[6];          // fac products: xx, yy, zz, xy, xz, yz
+  double* bp[3];         // out: adjoint of the plus / minus derivative per axis (fill box)
+  double* bm[3];
+  double* cc;            // out: 9 arrays of npts, the curvature's partials (see k_adj_curv)
   double* adj_vel;       // += dRHS/dvel * weight
-  double* lam_out;       // target of the carried-term scatter
   int64_t npts;
 };
 
-__global__ void __launch_bounds__(128) k_adj_rhs(AdjRhsArgs a) {
+// Per fill-box voxel: the adjoints of the six one-sided WENO5 derivatives
+// (Godunov normal term and upwind advection) and the partials of the
+// curvature term b kappa (3d.f:2336-2378) with respect to its ten central
+// differences, each times the voxel's adjoint weight.  Voxels whose normal
+// term is carried from an earlier voxel leave that term to k_adj_carry.
+__global__ void __launch_bounds__(128) k_adj_point(AdjPointArgs a) {
   const Box& b = a.b;
   const int i = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = b.jlo + blockIdx.y * blockDim.y + threadIdx.y;
   const int k = b.klo + blockIdx.z * blockDim.z + threadIdx.z;
   if (i > b.ihi || j > b.jhi || k > b.khi) return;
   const int64_t q = b.idx(i, j, k);
-  const double w = a.wgt[q];
-  double g[kOff];
-#pragma unroll
-  for (int o = 0; o < kOff; o++) g[o] = 0.0;
+  const double w = a.coef_l * a.lam_in[q];
   const int64_t st[3] = {1, (int64_t)b.nx, (int64_t)b.nx * b.ny};
   const double* __restrict__ phi = a.phi;
-  // forward values of the axis derivatives (for the upwind choices)
   double pp[3], pm[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     pp[d] = a.dp[d][q];
     pm[d] = a.dm[d][q];
   }
-  // Godunov normal term (or the carried term of an earlier voxel)
   const double vel = a.vel_n[q];
   double ppb[3] = {0, 0, 0}, pmb[3] = {0, 0, 0};
-  const bool own = fabs(vel) >= 1.e-5;
-  if (own) {
+  if (fabs(vel) >= 1.e-5) {
     double velb;
     godunov_bwd(vel, pp, pm, ppb, pmb, velb);
     a.adj_vel[q] += w * velb;
   }
-  // advection
   const double vxyz[3] = {a.vx[q], a.vy[q], a.vz[q]};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (qss_emu::ge0(vxyz[d])) pmb[d] += -vxyz[d];
     else ppb[d] += -vxyz[d];
+    a.bp[d][q] = w * ppb[d];
+    a.bm[d][q] = w * pmb[d];
   }
-  // chain the axis derivatives to the stencil
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    double P[7], Pb[7];
-#pragma unroll
-    for (int m = 0; m < 7; m++) {
-      P[m] = phi[q + (m - 3) * st[d]];
-      Pb[m] = 0.0;
-    }
-    weno_axis_bwd(P, a.inv[d], ppb[d], pmb[d], Pb);
-#pragma unroll
-    for (int m = 0; m < 7; m++) {
-      if (m == 3) g[0] += Pb[m];
-      else g[axis_off(d, m - 3)] += Pb[m];
-    }
-  }
-  // curvature b kappa (3d.f:2336-2378)
+  double out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   {
     const double fx = a.fac[0], fy = a.fac[1], fz = a.fac[2];
-    const double cc = phi[q];
+    // first differences as the forward computes them (the threshold test on
+    // their squares must take the forward's branch)
     const double phx = (phi[q + st[0]] - phi[q - st[0]]) * fx;
     const double phy = (phi[q + st[1]] - phi[q - st[1]]) * fy;
     const double phz = (phi[q + st[2]] - phi[q - st[2]]) * fz;
-    const double pxx = (phi[q + 2 * st[0]] + phi[q - 2 * st[0]] - 2 * cc) * fx * fx;
-    const double pyy = (phi[q + 2 * st[1]] + phi[q - 2 * st[1]] - 2 * cc) * fy * fy;
-    const double pzz = (phi[q + 2 * st[2]] + phi[q - 2 * st[2]] - 2 * cc) * fz * fz;
-    const double pxy = (phi[q + st[0] + st[1]] + phi[q - st[0] - st[1]] - phi[q - st[0] + st[1]] -
-                        phi[q + st[0] - st[1]]) * fx * fy;
-    const double pxz = (phi[q + st[0] + st[2]] + phi[q - st[0] - st[2]] - phi[q - st[0] + st[2]] -
-                        phi[q + st[0] - st[2]]) * fx * fz;
-    const double pyz = (phi[q + st[1] + st[2]] + phi[q - st[1] - st[2]] - phi[q - st[1] + st[2]] -
-                        phi[q + st[1] - st[2]]) * fy * fz;
-    const double grad = phx * phx + phy * phy + phz * phz;
-    if (qss_emu::bits(grad) >= qss_emu::bits(1.e-5)) {  // grad >= 1e-5 (a sum of squares)
-      const double curv = pxx * phy * phy + pyy * phx * phx - 2 * pxy * phx * phy + pxx * phz * phz +
-                          pzz * phx * phx - 2 * pxz * phx * phz + pyy * phz * phz + pzz * phy * phy -
-                          2 * pyz * phy * phz;
-      const double kb = a.bcoef[q];
+    const double grad = __dadd_rn(__dadd_rn(__dmul_rn(phx, phx), __dmul_rn(phy, phy)), __dmul_rn(phz, phz));
+    if (w != 0.0 && qss_emu::bits(grad) >= qss_emu::bits(1.e-5)) {  // grad >= 1e-5 (a sum of squares)
+      const double cc = phi[q];
+      const double pxx = (phi[q + 2 * st[0]] + phi[q - 2 * st[0]] - 2 * cc) * a.f2[0];
+      const double pyy = (phi[q + 2 * st[1]] + phi[q - 2 * st[1]] - 2 * cc) * a.f2[1];
+      const double pzz = (phi[q + 2 * st[2]] + phi[q - 2 * st[2]] - 2 * cc) * a.f2[2];
+      const double pxy = (phi[q + st[0] + st[1]] + phi[q - st[0] - st[1]] - phi[q - st[0] + st[1]] -
+                          phi[q + st[0] - st[1]]) * a.f2[3];
+      const double pxz = (phi[q + st[0] + st[2]] + phi[q - st[0] - st[2]] - phi[q - st[0] + st[2]] -
+                          phi[q + st[0] - st[2]]) * a.f2[4];
+      const double pyz = (phi[q + st[1] + st[2]] + phi[q - st[1] - st[2]] - phi[q - st[1] + st[2]] -
+                          phi[q + st[1] - st[2]]) * a.f2[5];
+      const double sx = phx * phx, sy = phy * phy, sz = phz * phz;
+      // kappa numerator (3d.f:2336-2378), regrouped
+      const double curv = pxx * (sy + sz) + pyy * (sx + sz) + pzz * (sx + sy) -
+                          2 * (pxy * phx * phy + pxz * phx * phz + pyz * phy * phz);
       const double ig = qss_emu::div(1.0, grad);
-      const double cb = kb * ig, gb = -kb * curv * ig * ig;
-      const double xb = cb * (2 * pyy * phx - 2 * pxy * phy + 2 * pzz * phx - 2 * pxz * phz) + gb * 2 * phx;
-      const double yb = cb * (2 * pxx * phy - 2 * pxy * phx + 2 * pzz * phy - 2 * pyz * phz) + gb * 2 * phy;
-      const double zb = cb * (2 * pxx * phz - 2 * pxz * phx + 2 * pyy * phz - 2 * pyz * phy) + gb * 2 * phz;
-      const double xxb = cb * (phy * phy + phz * phz) * fx * fx;
-      const double yyb = cb * (phx * phx + phz * phz) * fy * fy;
-      const double zzb = cb * (phx * phx + phy * phy) * fz * fz;
-      const double xyb = cb * (-2 * phx * phy) * fx * fy;
-      const double xzb = cb * (-2 * phx * phz) * fx * fz;
-      const double yzb = cb * (-2 * phy * phz) * fy * fz;
-      g[axis_off(0, 1)] += xb * fx;
-      g[axis_off(0, -1)] -= xb * fx;
-      g[axis_off(1, 1)] += yb * fy;
-      g[axis_off(1, -1)] -= yb * fy;
-      g[axis_off(2, 1)] += zb * fz;
-      g[axis_off(2, -1)] -= zb * fz;
-      g[axis_off(0, 2)] += xxb;
-      g[axis_off(0, -2)] += xxb;
-      g[axis_off(1, 2)] += yyb;
-      g[axis_off(1, -2)] += yyb;
-      g[axis_off(2, 2)] += zzb;
-      g[axis_off(2, -2)] += zzb;
-      g[0] -= 2 * (xxb + yyb + zzb);
-      g[19] += xyb;
-      g[20] += xyb;
-      g[21] -= xyb;
-      g[22] -= xyb;
-      g[23] += xzb;
-      g[24] += xzb;
-      g[25] -= xzb;
-      g[26] -= xzb;
-      g[27] += yzb;
-      g[28] += yzb;
-      g[29] -= yzb;
-      g[30] -= yzb;
+      const double cb = w * a.bcoef[q] * ig;  // d RHS / d numerator
+      const double gb = -cb * curv * ig;      // d RHS / d grad
+      out[0] = 2 * (phx * (cb * (pyy + pzz) + gb) - cb * (pxy * phy + pxz * phz)) * fx;
+      out[1] = 2 * (phy * (cb * (pxx + pzz) + gb) - cb * (pxy * phx + pyz * phz)) * fy;
+      out[2] = 2 * (phz * (cb * (pxx + pyy) + gb) - cb * (pxz * phx + pyz * phy)) * fz;
+      out[3] = cb * (sy + sz) * a.f2[0];
+      out[4] = cb * (sx + sz) * a.f2[1];
+      out[5] = cb * (sx + sy) * a.f2[2];
+      const double m2cb = -2 * cb;
+      out[6] = m2cb * phx * phy * a.f2[3];
+      out[7] = m2cb * phx * phz * a.f2[4];
+      out[8] = m2cb * phy * phz * a.f2[5];
     }
   }
 #pragma unroll
-  for (int o = 0; o < kOff; o++) a.contrib[o * a.npts + q] = w * g[o];
-  // carried normal term: its partials belong to the source voxel's stencil
-  if (!own && w != 0.0) {
-    const int src = a.nsrc[q];
-    if (src >= 0) {
-      double sp[3], sm[3];
+  for (int o = 0; o < 9; o++) a.cc[o * a.npts + q] = out[o];
+}
+
+// Voxels whose normal term is carried from an earlier voxel (|vel_n| < 1e-5,
+// 3d.f:459-486): their weight times the source voxel's Godunov partials goes
+// to the source's derivative adjoints (atomics; such voxels are rare).  Runs
+// after k_adj_point, which writes the source's own values.
+__global__ void __launch_bounds__(128) k_adj_carry(AdjPointArgs a) {
+  const Box& b = a.b;
+  const int i = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = b.jlo + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = b.klo + blockIdx.z * blockDim.z + threadIdx.z;
+  if (i > b.ihi || j > b.jhi || k > b.khi) return;
+  const int64_t q = b.idx(i, j, k);
+  if (fabs(a.vel_n[q]) >= 1.e-5) return;
+  const double w = a.coef_l * a.lam_in[q];
+  const int src = a.nsrc[q];
+  if (w == 0.0 || src < 0) return;
+  double sp[3], sm[3];
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        sp[d] = a.dp[d][src];
-        sm[d] = a.dm[d][src];
-      }
-      double spb[3] = {0, 0, 0}, smb[3] = {0, 0, 0}, velb;
-      godunov_bwd(a.vel_n[src], sp, sm, spb, smb, velb);
-      atomicAdd(a.adj_vel + src, w * velb);
+  for (int d = 0; d < 3; d++) {
+    sp[d] = a.dp[d][src];
+    sm[d] = a.dm[d][src];
+  }
+  double spb[3] = {0, 0, 0}, smb[3] = {0, 0, 0}, velb;
+  godunov_bwd(a.vel_n[src], sp, sm, spb, smb, velb);
+  atomicAdd(a.adj_vel + src, w * velb);
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        double P[7], Pb[7];
-#pragma unroll
-        for (int m = 0; m < 7; m++) {
-          P[m] = phi[src + (m - 3) * st[d]];
-          Pb[m] = 0.0;
-        }
-        weno_axis_bwd(P, a.inv[d], spb[d], smb[d], Pb);
-#pragma unroll
-        for (int m = 0; m < 7; m++) atomicAdd(a.lam_out + src + (m - 3) * st[d], w * Pb[m]);
-      }
-    }
+  for (int d = 0; d < 3; d++) {
+    if (spb[d] != 0.0) atomicAdd(a.bp[d] + src, w * spb[d]);
+    if (smb[d] != 0.0) atomicAdd(a.bm[d] + src, w * smb[d]);
   }
 }
 
-// lam_out[p] = coef * lam_in[p] (fill box) + sum over offsets of contrib[o][p - off(o)]
-__global__ void k_adj_gather(Box b, const double* __restrict__ contrib, int64_t npts, const double* lam_in,
-                             double coef, double* lam_out) {
+// Reverse of the WENO5 one-sided derivatives along one axis (3d.f:1968-2138),
+// one face window at a time.  With v(m) = (phi(m) - phi(m-1)) inv the scaled
+// difference of face m, the minus derivative of voxel c and the plus
+// derivative of voxel c-1 are the same WENO5 reconstruction of the window
+// u0..u4 = v(c-2..c+2), read in opposite directions: they share the three
+// smoothness indicators (S1+ = S3-, S2+ = S2-, S3+ = S1-) and eps, and
+// differ in the ideal weights (0.1, 0.6, 0.3 against 0.3, 0.6, 0.1 on
+// S1, S2, S3) and the candidate stencils.  Per window the adjoints of both
+// (the minus adjoint of voxel c, the plus adjoint of voxel c-1) are pushed
+// to the five faces at once:
+//   d value / d T_k = -2 w_k (p_k - value) / T_k,   T_k = S_k + eps,
+//   d value / d p_k = w_k,  d eps / d u_j = 2e-6 u_j at the maximum square
+// (the later operand of the reference's MAX chain on ties, per side).
+// Each thread owns one of nseg equal segments of a line's points and
+// recomputes the windows on either side of it whose faces it needs, so every
+// point's adjoint is written once, in a fixed order: lam(p) += inv (F(p) -
+// F(p+1)), F the face adjoints.
+struct AdjAxisArgs {
+  Box b;
+  const double* phi;
+  const double* bp;
+  const double* bm;
+  double* lam;
+  double inv;
+  int nseg;
+};
+
+template <int AX>
+__global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
+  const Box& b = a.b;
+  int p, q, lo, hi;
+  if (AX == 0) {
+    p = b.jlo + blockIdx.x * blockDim.x + threadIdx.x;  // j
+    q = b.klo + blockIdx.y;                              // k
+    if (p > b.jhi) return;
+    lo = b.ilo;
+    hi = b.ihi;
+  } else {
+    p = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;  // i
+    q = (AX == 1 ? b.klo : b.jlo) + blockIdx.y;
+    if (p > b.ihi) return;
+    lo = (AX == 1) ? b.jlo : b.klo;
+    hi = (AX == 1) ? b.jhi : b.khi;
+  }
+  const int len = hi - lo + 7;  // points lo-3 .. hi+3
+  const int p0 = lo - 3 + (int)(((int64_t)blockIdx.z * len) / a.nseg);
+  const int pend = lo - 3 + (int)(((int64_t)(blockIdx.z + 1) * len) / a.nseg) - 1;
+  if (pend < p0) return;
+  int64_t base, stride;
+  if (AX == 0) {
+    base = b.idx(0, p, q);
+    stride = 1;
+  } else if (AX == 1) {
+    base = b.idx(p, 0, q);
+    stride = b.nx;
+  } else {
+    base = b.idx(p, q, 0);
+    stride = (int64_t)b.nx * b.ny;
+  }
+  const double* __restrict__ phi = a.phi;
+  const double inv = a.inv;
+  const int last = (AX == 0 ? b.nx : (AX == 1 ? b.ny : b.nz)) - 1;
+  // loads outside the line only feed windows without adjoints
+  auto ld = [&](int m) -> double {
+    const int mm = m < 0 ? 0 : (m > last ? last : m);
+    return __ldg(phi + base + (int64_t)mm * stride);
+  };
+  auto ldbar = [&](const double* arr, int m) -> double {
+    return (m >= lo && m <= hi) ? __ldg(arr + base + (int64_t)m * stride) : 0.0;
+  };
+  using qss_emu::bits;
+  // window c = p0 - 2 first: faces c-2 .. c+1 now, face c+2 in the loop
+  const int c0 = p0 - 2;
+  double f_m3 = ld(c0 - 3), f_m2 = ld(c0 - 2), f_m1 = ld(c0 - 1), f_0 = ld(c0), f_p1 = ld(c0 + 1);
+  double u0 = (f_m2 - f_m3) * inv, u1 = (f_m1 - f_m2) * inv, u2 = (f_0 - f_m1) * inv, u3 = (f_p1 - f_0) * inv;
+  double s0 = u0 * u0, s1 = u1 * u1, s2 = u2 * u2, s3 = u3 * u3;
+  double plast = f_p1;
+  double F0 = 0, F1 = 0, F2 = 0, F3 = 0, F4 = 0;  // adjoints of faces c-2 .. c+2
+  double prevF = 0;                                // completed adjoint of face c-3
+  // the second difference a(m) = v(m-1) - 2 v(m) + v(m+1) of centre m and its
+  // term 13/12 a^2 enter S1 of window m+1, S2 of window m and S3 of window
+  // m-1: kept for centres c-1, c (c+1 computed per window), their adjoints
+  // summed over the three windows
+  double am_ = (u0 - 2.0 * u1) + u2, a0_ = (u1 - 2.0 * u2) + u3;
+  double Am_ = k1312 * (am_ * am_), A0_ = k1312 * (a0_ * a0_);
+  double BAm = 0, BA0 = 0, BAp = 0;  // adjoints of the terms of centres c-1, c, c+1
+#pragma unroll 1
+  for (int c = c0; c <= pend + 3; c++) {
+    const double pn = ld(c + 2);
+    const double u4 = (pn - plast) * inv;
+    plast = pn;
+    const double s4 = u4 * u4;
+    const double ap_ = (u2 - 2.0 * u3) + u4;
+    const double Ap_ = k1312 * (ap_ * ap_);
+    const double gm = ldbar(a.bm, c), gp = ldbar(a.bp, c - 1);
+    if (gm != 0.0 || gp != 0.0) {
+      // eps and the position of the largest square for each reading direction
+      const long long b0 = (long long)bits(s0), b1 = (long long)bits(s1), b2 = (long long)bits(s2),
+                      b3 = (long long)bits(s3), b4 = (long long)bits(s4);
+      long long mx = b0;
+      int im = 0;  // minus: u0 .. u4, later wins ties
+      if (b1 >= mx) { mx = b1; im = 1; }
+      if (b2 >= mx) { mx = b2; im = 2; }
+      if (b3 >= mx) { mx = b3; im = 3; }
+      if (b4 >= mx) { mx = b4; im = 4; }
+      long long mp = b4;
+      int ip = 4;  // plus: u4 .. u0, later wins ties
+      if (b3 >= mp) { mp = b3; ip = 3; }
+      if (b2 >= mp) { mp = b2; ip = 2; }
+      if (b1 >= mp) { mp = b1; ip = 1; }
+      if (b0 >= mp) { mp = b0; ip = 0; }
+      const double eps = 1e-6 * qss_emu::from_bits((unsigned long long)mx) + 1.0e-35;
+      const double b1t = (u0 - 4.0 * u1) + 3.0 * u2, e2 = u1 - u3, b3t = (3.0 * u2 - 4.0 * u3) + u4;
+      const double S1 = Am_ + 0.25 * (b1t * b1t);
+      const double S2 = A0_ + 0.25 * (e2 * e2);
+      const double S3 = Ap_ + 0.25 * (b3t * b3t);
+      const double r1 = qss_emu::div(1.0, S1 + eps), r2 = qss_emu::div(1.0, S2 + eps),
+                   r3 = qss_emu::div(1.0, S3 + eps);
+      const double q1 = r1 * r1, q2 = r2 * r2, q3 = r3 * r3;
+      const double am2 = 0.6 * q2;
+      const double am1 = 0.1 * q1, am3 = 0.3 * q3;  // minus: 0.1, 0.6, 0.3
+      const double ap1 = 0.3 * q1, ap3 = 0.1 * q3;  // plus (on S1, S2, S3): 0.3, 0.6, 0.1
+      const double iam = qss_emu::div(1.0, am1 + am2 + am3), iap = qss_emu::div(1.0, ap1 + am2 + ap3);
+      const double wm1 = am1 * iam, wm2 = am2 * iam, wm3 = am3 * iam;
+      const double wp1 = ap1 * iap, wp2 = am2 * iap, wp3 = ap3 * iap;
+      // candidate stencils: minus reads u0..u4, plus reads u4..u0
+      const double pm1 = kC13 * u0 - kC76 * u1 + kC116 * u2;
+      const double pm2 = -kC16 * u1 + kC56 * u2 + kC13 * u3;
+      const double pm3 = kC13 * u2 + kC56 * u3 - kC16 * u4;
+      const double pq1 = -kC16 * u0 + kC56 * u1 + kC13 * u2;  // plus stencil on S1 (its third)
+      const double pq2 = kC13 * u1 + kC56 * u2 - kC16 * u3;   // on S2
+      const double pq3 = kC116 * u2 - kC76 * u3 + kC13 * u4;  // on S3 (its first)
+      const double vm = wm1 * pm1 + wm2 * pm2 + wm3 * pm3;
+      const double vp = wp1 * pq1 + wp2 * pq2 + wp3 * pq3;
+      const double P1 = gm * wm1, P2 = gm * wm2, P3 = gm * wm3;
+      const double Q1 = gp * wp1, Q2 = gp * wp2, Q3 = gp * wp3;
+      const double x1 = qss_emu::scale2(r1, 1), x2 = qss_emu::scale2(r2, 1), x3 = qss_emu::scale2(r3, 1);
+      // x_k = 2 r_k; the minus sign of d value / d T_k is folded into the differences
+      const double m1 = P1 * (vm - pm1) * x1, m2 = P2 * (vm - pm2) * x2, m3 = P3 * (vm - pm3) * x3;
+      const double n1 = Q1 * (vp - pq1) * x1, n2 = Q2 * (vp - pq2) * x2, n3 = Q3 * (vp - pq3) * x3;
+      const double bS1 = m1 + n1, bS2 = m2 + n2, bS3 = m3 + n3;
+      const double bem = m1 + m2 + m3, bep = n1 + n2 + n3;
+      BAm += bS1;
+      BA0 += bS2;
+      BAp += bS3;
+      const double bb1 = bS1 * qss_emu::scale2(b1t, -1);
+      const double be2 = bS2 * qss_emu::scale2(e2, -1);
+      const double bb3 = bS3 * qss_emu::scale2(b3t, -1);
+      double d0 = bb1 + kC13 * P1 - kC16 * Q1;
+      double d1 = -4.0 * bb1 + be2 - kC76 * P1 - kC16 * P2 + kC56 * Q1 + kC13 * Q2;
+      double d2 = 3.0 * bb1 + 3.0 * bb3 + kC116 * P1 + kC56 * P2 + kC13 * P3 + kC13 * Q1 + kC56 * Q2 +
+                  kC116 * Q3;
+      double d3 = -be2 - 4.0 * bb3 + kC13 * P2 + kC56 * P3 - kC16 * Q2 - kC76 * Q3;
+      double d4 = bb3 - kC16 * P3 + kC13 * Q3;
+      // eps = 1e-6 max(u^2) + 1e-35, per reading direction
+      {
+        // both directions usually pick the same face: one sum, then selects
+        const double um = im == 0 ? u0 : im == 1 ? u1 : im == 2 ? u2 : im == 3 ? u3 : u4;
+        const double up = ip == 0 ? u0 : ip == 1 ? u1 : ip == 2 ? u2 : ip == 3 ? u3 : u4;
+        const double cm = 2e-6 * um * bem, cp = 2e-6 * up * bep;
+        const double cs = (im == ip) ? cm + cp : cm;
+        auto ex = [&](int j) { return j == im ? cs : (j == ip && im != ip ? cp : 0.0); };
+        d0 += ex(0);
+        d1 += ex(1);
+        d2 += ex(2);
+        d3 += ex(3);
+        d4 += ex(4);
+      }
+      F0 += d0;
+      F1 += d1;
+      F2 += d2;
+      F3 += d3;
+      F4 += d4;
+    }
+    // centre c-1 is complete: its term 13/12 a^2 back to faces c-2, c-1, c
+    {
+      const double ba = BAm * (k136 * am_);
+      F0 += ba;
+      F1 -= 2.0 * ba;
+      F2 += ba;
+    }
+    // face c-2 is complete: the point between faces c-3 and c-2 is done
+    const int m = c - 2;
+    if (m > p0) {
+      const int pt = m - 1;
+      double* l = a.lam + base + (int64_t)pt * stride;
+      *l += inv * (prevF - F0);
+    }
+    prevF = F0;
+    // slide the window by one face
+    u0 = u1;
+    u1 = u2;
+    u2 = u3;
+    u3 = u4;
+    s0 = s1;
+    s1 = s2;
+    s2 = s3;
+    s3 = s4;
+    F0 = F1;
+    F1 = F2;
+    F2 = F3;
+    F3 = F4;
+    F4 = 0;
+    am_ = a0_;
+    a0_ = ap_;
+    Am_ = A0_;
+    A0_ = Ap_;
+    BAm = BA0;
+    BA0 = BAp;
+    BAp = 0;
+  }
+}
+
+// lam_out[p] += coef * lam_in[p] (fill box) + the curvature partials of the
+// fill-box voxels whose central stencil holds p, in a fixed order:
+//   cc[0..2] first derivatives (+ at p-e, - at p+e), cc[3..5] second
+//   derivatives (+ at p -+ 2e, -2 at p), cc[6..8] mixed xy, xz, yz
+//   (+ at p -+ (e1 + e2), - at p + (e1 - e2) and p - (e1 - e2))
+__global__ void k_adj_curv(Box b, const double* __restrict__ cc, int64_t npts, const double* lam_in, double coef,
+                           double* lam_out) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts; p += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(p % b.nx);
     const int64_t r = p / b.nx;
     const int j = (int)(r % b.ny), k = (int)(r / b.ny);
-    const bool fill = i >= b.ilo && i <= b.ihi && j >= b.jlo && j <= b.jhi && k >= b.klo && k <= b.khi;
-    double s = fill ? coef * lam_in[p] : 0.0;
-    for (int o = 0; o < kOff; o++) {
-      int di, dj, dk;
-      offset_of(o, di, dj, dk);
-      const int qi = i - di, qj = j - dj, qk = k - dk;
-      if (qi < b.ilo || qi > b.ihi || qj < b.jlo || qj > b.jhi || qk < b.klo || qk > b.khi) continue;
-      s += contrib[o * npts + b.idx(qi, qj, qk)];
-    }
+    auto in_fill = [&](int ii, int jj, int kk) {
+      return ii >= b.ilo && ii <= b.ihi && jj >= b.jlo && jj <= b.jhi && kk >= b.klo && kk <= b.khi;
+    };
+    auto at = [&](int o, int di, int dj, int dk) -> double {
+      const int ii = i + di, jj = j + dj, kk = k + dk;
+      return in_fill(ii, jj, kk) ? cc[o * npts + b.idx(ii, jj, kk)] : 0.0;
+    };
+    double s = in_fill(i, j, k) ? coef * lam_in[p] : 0.0;
+    s += at(0, -1, 0, 0) - at(0, 1, 0, 0);
+    s += at(1, 0, -1, 0) - at(1, 0, 1, 0);
+    s += at(2, 0, 0, -1) - at(2, 0, 0, 1);
+    s += at(3, -2, 0, 0) + at(3, 2, 0, 0) - 2.0 * at(3, 0, 0, 0);
+    s += at(4, 0, -2, 0) + at(4, 0, 2, 0) - 2.0 * at(4, 0, 0, 0);
+    s += at(5, 0, 0, -2) + at(5, 0, 0, 2) - 2.0 * at(5, 0, 0, 0);
+    s += at(6, -1, -1, 0) + at(6, 1, 1, 0) - at(6, 1, -1, 0) - at(6, -1, 1, 0);
+    s += at(7, -1, 0, -1) + at(7, 1, 0, 1) - at(7, 1, 0, -1) - at(7, -1, 0, 1);
+    s += at(8, 0, -1, -1) + at(8, 0, 1, 1) - at(8, 0, 1, -1) - at(8, 0, -1, 1);
     lam_out[p] += s;
   }
 }
@@ -670,7 +740,7 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
       }
       size_t free_b = 0, total_b = 0;
       QSS_CK(cudaMemGetInfo(&free_b, &total_b));
-      const double need = (double)ckpt * 18 * bytes + (double)(kOff + 8) * bytes;
+      const double need = (double)ckpt * 18 * bytes + (double)(15 + 8) * bytes;
       if (need < 0.6 * (double)free_b) {
         sder.resize(ckpt);
         for (auto& sd : sder)
@@ -721,7 +791,9 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
       return 0;
     }
     // backward
-    double* contrib = buf.get((int64_t)kOff * n);
+    double* bars = buf.get(6 * n);  // adjoints of the plus / minus derivatives per axis
+    double* cc = buf.get(9 * n);    // curvature partials
+    launch_fill(a.s, 9 * n, cc, 0.0);  // outside the fill box they stay zero
     double* adj_vel = buf.get(n);
     double* lam3 = buf.get(n);
     double* lam2 = buf.get(n);
@@ -730,7 +802,7 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
     double* wgt = buf.get(n);
     double* gth = buf.get(n);
     launch_fill(a.s, n, adj_vel, 0.0);
-    AdjRhsArgs ar;
+    AdjPointArgs ar;
     ar.b = b;
     ar.vel_n = vel;
     ar.bcoef = bco;
@@ -738,15 +810,39 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
     ar.vy = vv[1];
     ar.vz = vv[2];
     ar.nsrc = nsrc;
+    for (int d = 0; d < 3; d++) ar.fac[d] = 0.5 / g->dx[d];
+    ar.f2[0] = ar.fac[0] * ar.fac[0];
+    ar.f2[1] = ar.fac[1] * ar.fac[1];
+    ar.f2[2] = ar.fac[2] * ar.fac[2];
+    ar.f2[3] = ar.fac[0] * ar.fac[1];
+    ar.f2[4] = ar.fac[0] * ar.fac[2];
+    ar.f2[5] = ar.fac[1] * ar.fac[2];
     for (int d = 0; d < 3; d++) {
-      ar.inv[d] = 1.0 / g->dx[d];
-      ar.fac[d] = 0.5 / g->dx[d];
+      ar.bp[d] = bars + (int64_t)d * n;
+      ar.bm[d] = bars + (int64_t)(3 + d) * n;
     }
-    ar.contrib = contrib;
+    ar.cc = cc;
     ar.adj_vel = adj_vel;
     ar.npts = n;
     const dim3 blk(32, 4, 1);
     const dim3 grd((b.fbx() + 31) / 32, (b.fby() + 3) / 4, b.fbz());
+    // line kernels: lanes along i for the y and z passes, along j for x; each
+    // line cut into equal segments of at least 32 points (the windows a
+    // segment recomputes at its ends cost 5 per segment), enough of them for
+    // about two waves of 20 warps per SM
+    auto nseg_of = [&](int ax) {
+      const int len = (ax == 0 ? b.fbx() : ax == 1 ? b.fby() : b.fbz()) + 6;
+      const int64_t lines = (ax == 0) ? (int64_t)b.fby() * b.fbz()
+                                      : (ax == 1 ? (int64_t)b.fbx() * b.fbz() : (int64_t)b.fbx() * b.fby());
+      const int64_t want = 2LL * 152 * 20 * 32;
+      int64_t ns = (want + lines - 1) / lines;
+      if (ns > len / 32) ns = len / 32;
+      return (int)(ns < 1 ? 1 : ns);
+    };
+    const int ns0 = nseg_of(0), ns1 = nseg_of(1), ns2 = nseg_of(2);
+    const dim3 ag0((unsigned)((b.fby() + 127) / 128), (unsigned)b.fbz(), (unsigned)ns0);
+    const dim3 ag1((unsigned)((b.fbx() + 127) / 128), (unsigned)b.fbz(), (unsigned)ns1);
+    const dim3 ag2((unsigned)((b.fbx() + 127) / 128), (unsigned)b.fby(), (unsigned)ns2);
     auto bc_bwd = [&](const double* val, double* l) {
       const int n2 = b.nx * b.ny, n1 = b.nx * b.fbz(), n0 = b.fby() * b.fbz();
       k_adj_bc<<<(n2 + 255) / 256, 256, 0, a.s>>>(b, 2, val, l);
@@ -769,12 +865,28 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
           ar.dm[d] = a.dm[d];
         }
       }
-      k_scale_fill<<<g1(n), 256, 0, a.s>>>(b, lam_in, coef_l, wgt);
       ar.phi = in;
-      ar.wgt = wgt;
-      ar.lam_out = lam_out;
-      k_adj_rhs<<<grd, blk, 0, a.s>>>(ar);
-      k_adj_gather<<<g1(n), 256, 0, a.s>>>(b, contrib, n, lam_in, coef_id, lam_out);
+      ar.lam_in = lam_in;
+      ar.coef_l = coef_l;
+      k_adj_point<<<grd, blk, 0, a.s>>>(ar);
+      k_adj_carry<<<grd, blk, 0, a.s>>>(ar);
+      AdjAxisArgs ax{b, in, nullptr, nullptr, lam_out, 0.0, 1};
+      ax.bp = ar.bp[0];
+      ax.bm = ar.bm[0];
+      ax.inv = 1.0 / g->dx[0];
+      ax.nseg = ns0;
+      k_adj_axis<0><<<ag0, 128, 0, a.s>>>(ax);
+      ax.bp = ar.bp[1];
+      ax.bm = ar.bm[1];
+      ax.inv = 1.0 / g->dx[1];
+      ax.nseg = ns1;
+      k_adj_axis<1><<<ag1, 128, 0, a.s>>>(ax);
+      ax.bp = ar.bp[2];
+      ax.bm = ar.bm[2];
+      ax.inv = 1.0 / g->dx[2];
+      ax.nseg = ns2;
+      k_adj_axis<2><<<ag2, 128, 0, a.s>>>(ax);
+      k_adj_curv<<<g1(n), 256, 0, a.s>>>(b, cc, n, lam_in, coef_id, lam_out);
     };
     for (int k = nseg - 1; k >= 0; k--) {
       const int s0 = k * ckpt, s1 = std::min(nsteps, s0 + ckpt);

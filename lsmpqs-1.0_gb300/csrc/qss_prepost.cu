@@ -4,6 +4,7 @@
 //   qssgpu_create_mask_ubc        src/applications/createMaskUBC.c:76-112
 //   qssgpu_create_init_from_mask  src/applications/createInitFromMask.c:55-85 (3-D)
 //   qssgpu_diff_steps             src/applications/makeDiffSteps.c:54-132 (3-D)
+//   qssgpu_phase_uchar            src/applications/makeRaw.c:52-135 (phase images)
 //
 // The reference runs these as command-line programs (or, for the mask
 // reinitialisation, a library routine they call); here each is one library
@@ -46,6 +47,37 @@ __global__ void k_diff(int64_t n, const double* __restrict__ a, const double* __
     p = (m > p) ? m : p;
     phi[q] = p;
     bin[q] = (p < 0.0) ? 1 : 0;
+  }
+}
+
+// makeRaw's 0/1 phase images: bin = (f < 0) (IMPOSE_UCHAR, qss_macros.h:97-104)
+// of f = mask (phase 'm', makeRaw.c:96), phi ('n', :107) or max(mask, -phi)
+// ('w': COPY_DATA, NEGATE_DATA, IMPOSE_MASK, :123-128, qss_macros.h:56-86);
+// the ghost-box image and/or the fill box packed i fastest (copyDataFB,
+// makeRaw.c:52-73)
+__global__ void k_phase_uchar(Box b, const double* __restrict__ phi, const double* __restrict__ mask, int phase,
+                              unsigned char* full, unsigned char* fb) {
+  const int64_t n = b.npts();
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    double f;
+    if (phase == 'm') {
+      f = mask[q];
+    } else if (phase == 'n') {
+      f = phi[q];
+    } else {
+      const double s = -phi[q];
+      const double m = mask[q];
+      f = (m > s) ? m : s;
+    }
+    const unsigned char v = (f < 0) ? 1 : 0;
+    if (full) full[q] = v;
+    if (fb) {
+      const int i = (int)(q % b.nx);
+      const int64_t r = q / b.nx;
+      const int j = (int)(r % b.ny), k = (int)(r / b.ny);
+      if (i >= b.ilo && i <= b.ihi && j >= b.jlo && j <= b.jhi && k >= b.klo && k <= b.khi)
+        fb[(i - b.ilo) + (int64_t)b.fbx() * ((j - b.jlo) + (int64_t)b.fby() * (k - b.klo))] = v;
+    }
   }
 }
 
@@ -273,6 +305,38 @@ int qssgpu_diff_steps(const double* step_a, const double* step_b, Grid* g, doubl
       d2h(st.s, connected, phi, bytes);
       QSS_CK(cudaStreamSynchronize(st.s));
     }
+    return 0;
+  } catch (const Error& e) {
+    set_error(e.code, e.what());
+    return e.code ? e.code : 1;
+  }
+}
+
+// See include/lsmpqs_gpu.h.
+int qssgpu_phase_uchar(const double* phi, const double* mask, Grid* g, char phase, unsigned char* bin_full,
+                       unsigned char* bin_fb) {
+  try {
+    ensure_device();
+    validate_grid(g);
+    const bool need_phi = phase == 'n' || phase == 'w', need_mask = phase == 'm' || phase == 'w';
+    if ((phase != 'm' && phase != 'n' && phase != 'w') || (need_phi && !phi) || (need_mask && !mask) ||
+        (!bin_full && !bin_fb))
+      throw Error(QSSGPU_ERR_ARG, "qssgpu_phase_uchar: bad arguments");
+    const Box b = box_of(g);
+    const int64_t n = b.npts(), nfb = (int64_t)b.fbx() * b.fby() * b.fbz();
+    const size_t bytes = (size_t)n * sizeof(double);
+    Stream st;
+    Buf buf;
+    double* dphi = need_phi ? buf.get<double>(n) : nullptr;
+    double* dmask = need_mask ? buf.get<double>(n) : nullptr;
+    unsigned char* dfull = bin_full ? buf.get<unsigned char>(n) : nullptr;
+    unsigned char* dfb = bin_fb ? buf.get<unsigned char>(nfb) : nullptr;
+    if (dphi) h2d(st.s, dphi, phi, bytes);
+    if (dmask) h2d(st.s, dmask, mask, bytes);
+    k_phase_uchar<<<g1(n), 256, 0, st.s>>>(b, dphi, dmask, phase, dfull, dfb);
+    if (dfull) d2h(st.s, bin_full, dfull, (size_t)n);
+    if (dfb) d2h(st.s, bin_fb, dfb, (size_t)nfb);
+    QSS_CK(cudaStreamSynchronize(st.s));
     return 0;
   } catch (const Error& e) {
     set_error(e.code, e.what());

@@ -170,6 +170,10 @@ def load(path: str) -> C.CDLL:
         "qssgpu_create_init_from_mask": (C.c_int, [P(QSSDataArrays), P(Grid), P(Options)]),
         "qssgpu_diff_steps": (C.c_int, [P(C.c_double), P(C.c_double), P(Grid), P(C.c_double), P(C.c_double),
                                         P(C.c_int)]),
+        "qssgpu_phase_uchar": (C.c_int, [P(C.c_double), P(C.c_double), P(Grid), C.c_char, P(C.c_ubyte),
+                                         P(C.c_ubyte)]),
+        "oracle_phase_uchar": (C.c_int, [P(C.c_double), P(C.c_double), P(Grid), C.c_char, P(C.c_ubyte),
+                                         P(C.c_ubyte)]),
         "oracle_create_mask_ubc": (C.c_int, [P(C.c_ubyte), P(QSSDataArrays), P(Grid), P(Options)]),
         "oracle_create_init_from_mask": (C.c_int, [P(QSSDataArrays), P(Grid), P(Options)]),
         "oracle_diff_steps": (C.c_int, [P(C.c_double), P(C.c_double), P(Grid), P(C.c_double), P(C.c_double),

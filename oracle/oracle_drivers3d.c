@@ -16,9 +16,10 @@
  *   imbibe_model3d             src/level_set_evolution/imbibe_model3d.c:49-161
  *   reinitializeSubcellFix3d   src/reinitialization/reinitialize_top.c:297-377
  *   qss_reinitialize_mask      src/utilities/qss_general_util.c:261-306
- *   createMaskUBC, createInitFromMask, makeDiffSteps (logic of the CLIs)
+ *   createMaskUBC, createInitFromMask, makeDiffSteps, makeRaw (logic of the CLIs)
  *                              src/applications/createMaskUBC.c:76-112,
- *                              createInitFromMask.c:55-85, makeDiffSteps.c:54-132
+ *                              createInitFromMask.c:55-85, makeDiffSteps.c:54-132,
+ *                              makeRaw.c:52-135
  *   trapComponents_mask        src/connectivity/trapComponents.c:156-375
  *   findConnectivity3d         src/connectivity/connectivity.c:48-217
  *   getMainInd_new             src/connectivity/connectivity.c:219-296
@@ -545,6 +546,38 @@ int oracle_diff_steps(const double *a, const double *b, Grid *g, double *diff, d
   }
   free(q.phi_bin);
   free(q.connectivity);
+  return 0;
+}
+
+/* makeRaw.c:52-135: 0/1 image of f < 0 (IMPOSE_UCHAR) for f = mask ('m'),
+   phi ('n') or max(mask, -phi) ('w': COPY_DATA, NEGATE_DATA, IMPOSE_MASK);
+   full = ghost box, fb = fill box packed i fastest (copyDataFB)            */
+int oracle_phase_uchar(const double *phi, const double *mask, Grid *g, char phase, unsigned char *full,
+                       unsigned char *fb)
+{
+  int n = g->num_gridpts, nx = g->grid_dims_ghostbox[0], nxy = nx * g->grid_dims_ghostbox[1];
+  unsigned char *img = (unsigned char *)malloc((size_t)n);
+  double *s = (double *)malloc((size_t)n * sizeof(double));
+  if (phase == 'm') {
+    for (int i = 0; i < n; i++) img[i] = (mask[i] < 0) ? 1 : 0;
+  } else if (phase == 'n') {
+    for (int i = 0; i < n; i++) img[i] = (phi[i] < 0) ? 1 : 0;
+  } else {
+    for (int i = 0; i < n; i++) s[i] = phi[i];
+    for (int i = 0; i < n; i++) s[i] = -s[i];
+    for (int i = 0; i < n; i++) s[i] = (mask[i] > s[i]) ? mask[i] : s[i];
+    for (int i = 0; i < n; i++) img[i] = (s[i] < 0) ? 1 : 0;
+  }
+  if (full) memcpy(full, img, (size_t)n);
+  if (fb) {
+    int fx = g->ihi_fb - g->ilo_fb + 1, fy = g->jhi_fb - g->jlo_fb + 1;
+    for (int k = g->klo_fb; k <= g->khi_fb; k++)
+      for (int j = g->jlo_fb; j <= g->jhi_fb; j++)
+        for (int i = g->ilo_fb; i <= g->ihi_fb; i++)
+          fb[(i - g->ilo_fb) + (j - g->jlo_fb) * fx + (k - g->klo_fb) * fx * fy] = img[i + j * nx + k * nxy];
+  }
+  free(img);
+  free(s);
   return 0;
 }
 

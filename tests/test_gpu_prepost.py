@@ -80,3 +80,32 @@ def test_diff_steps(gpu, oracle, shift, expect):
     assert np.array_equal(res[0][0], res[1][0])
     assert res[0][2] == res[1][2] == expect
     assert np.array_equal(res[0][1], res[1][1])
+
+
+@pytest.mark.parametrize("phase", ["m", "n", "w"])
+def test_phase_uchar(gpu, oracle, phase):
+    """makeRaw's 0/1 phase images (ghost box and packed fill box) of the mask,
+    the non-wetting phase and the wetting phase, with exact and signed zeros
+    in phi and the mask."""
+    g, v = pack_case(oracle, 21, seed=13)
+    rng = np.random.default_rng(17)
+    phi = v["phi"].copy()
+    mask = v["mask"].copy()
+    for arr in (phi, mask):
+        sel = rng.random(arr.shape) < 0.05
+        arr[sel] = rng.choice([0.0, -0.0, 1e-300, -1e-300], sel.sum())
+    nfb = 21 ** 3
+    res = []
+    for lib, fn in ((gpu, "qssgpu_phase_uchar"), (oracle, "oracle_phase_uchar")):
+        full = np.full(v.shape, 7, dtype=np.uint8)
+        fb = np.full(nfb, 7, dtype=np.uint8)
+        rc = getattr(lib, fn)(Q.dptr(phi), Q.dptr(mask), C.byref(g), phase.encode(),
+                              full.ctypes.data_as(C.POINTER(C.c_ubyte)), fb.ctypes.data_as(C.POINTER(C.c_ubyte)))
+        assert rc == 0
+        res.append((full, fb))
+    Q.check(gpu)
+    assert np.array_equal(res[0][0], res[1][0])
+    assert np.array_equal(res[0][1], res[1][1])
+    assert set(np.unique(res[0][0])) <= {0, 1} and res[0][0].any()
+    # the packed image is the fill box of the full one
+    assert np.array_equal(res[0][1].reshape(21, 21, 21), res[0][0][3:24, 3:24, 3:24])
