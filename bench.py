@@ -484,9 +484,12 @@ def adjoint_arm(args):
     t_adj = time.perf_counter() - t0
     return {"n": n, "steps": steps, "checkpoint_every": ckpt, "loss": loss.value,
             "forward_s": t_fwd, "forward_and_gradient_s": t_adj, "adjoint_cost_over_forward": t_adj / t_fwd,
+            "backward_over_forward": (t_adj - t_fwd) / t_fwd,
             "forward_voxel_steps_per_s": n ** 3 * steps / t_fwd,
             "grad_abs_max": float(np.abs(grad).max()),
-            "note": "wall clock including uploads; gradient d loss / d theta per voxel (radians)"}
+            "note": "wall clock including uploads; adjoint_cost_over_forward = (forward + gradient) / forward, "
+                    "backward_over_forward = the backward pass (checkpoint recomputation + reverse sweep) / "
+                    "forward; gradient d loss / d theta per voxel (radians)"}
 
 
 def cpu_arm(args, nz: int, steps: int, warmup: int, threads: int):
