@@ -174,6 +174,7 @@ struct AxisArgs {
   double* dminus;
   double inv;
   const Ctl* ctl;
+  int seg_len;  // voxels per thread at EMU >= 1 (SEG at EMU 0)
 };
 
 // One thread: SEG consecutive voxels along axis AX starting at s0, inside
@@ -201,7 +202,8 @@ __global__ void __launch_bounds__(128) k_weno_axis(AxisArgs a) {
     lo = (AX == 1) ? b.jlo : b.klo;
     hi = (AX == 1) ? b.jhi : b.khi;
   }
-  const int s0 = lo + seg * SEG;
+  const int len = EMU == 0 ? SEG : a.seg_len;
+  const int s0 = lo + seg * len;
   if (s0 > hi) return;
   int64_t base, stride;
   if (AX == 0) {
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(128) k_weno_axis(AxisArgs a) {
   // fully unrolled, the loop with the integer-pipe arithmetic no longer fits
   // the instruction cache; the window then rotates by register moves
 #pragma unroll(EMU == 0 ? SEG : 1)
-  for (int t = 0; t < SEG; t++) {
+  for (int t = 0; t < (EMU == 0 ? SEG : len); t++) {
     const int i = s0 + t;
     // window: faces i-2 (fm2) .. i+2 (f2); centres i-1 (cm1) .. i+1 (c1)
     const double pnext = ld(i + 3);
@@ -443,11 +445,24 @@ template <int EMU>
 void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[3], double* const dp[3],
              double* const dm[3], const Ctl* ctl) {
   for (int ax = 0; ax < 3; ax++) {
-    AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl};
     const int along = ax == 0 ? b.fbx() : (ax == 1 ? b.fby() : b.fbz());
     const int lanes = ax == 0 ? b.fby() : b.fbx();
     const int other = ax == 2 ? b.fby() : b.fbz();
-    dim3 g((lanes + 127) / 128, other, (along + SEG - 1) / SEG);
+    // a segment recomputes 5 faces and 3 centres before its first voxel:
+    // segments as long as the line allows while the launch still fills
+    // about four waves of 12 warps on every SM (at least SEG voxels)
+    int len = SEG;
+    if (EMU != 0) {
+      const int64_t lines = (int64_t)lanes * other;
+      const int64_t want = 4LL * 152 * 12 * 32;
+      int64_t nseg = (want + lines - 1) / lines;
+      const int64_t most = (along + SEG - 1) / SEG;
+      if (nseg > most) nseg = most;
+      if (nseg < 1) nseg = 1;
+      len = (int)((along + nseg - 1) / nseg);
+    }
+    AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
+    dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
     cudaEvent_t e0 = ctl ? prof_open(s) : nullptr;
     if (ax == 0) k_weno_axis<0, EMU><<<g, 128, 0, s>>>(a);
     else if (ax == 1) k_weno_axis<1, EMU><<<g, 128, 0, s>>>(a);
