@@ -13,6 +13,7 @@
 #include <cstring>
 #include <initializer_list>
 #include <ctime>
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <string>
@@ -237,8 +238,14 @@ int qssgpu_ladder_batch(int drain, int n, Options* const* o, QSS_DataArrays* con
     }
     setup[v] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
+  // largest volumes first, so that no large volume starts last and runs alone
+  std::vector<int> order(n);
+  for (int v = 0; v < n; v++) order[v] = v;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return g[x]->num_gridpts > g[y]->num_gridpts; });
   auto work = [&]() {
-    for (int v = next++; v < n; v = next++) {
+    for (int k = next++; k < n; k = next++) {
+      const int v = order[k];
       if (codes[v]) continue;
       qssgpu_clear_error();
       try {
