@@ -232,16 +232,22 @@ def gpu_arm(args, dist: Dist):
     if args.e2e:
         wm, wp = make_workload(48)
         _e2e_call(lib, Q.make_grid(lib, 48), wm, wp, args.steps, dist)
-        r = _e2e_call(lib, g, v["mask"], v["phi"], args.steps, dist)
+        # the call is repeated on fresh host arrays and the median call
+        # reported: host page faults make single calls vary by ~10 %
+        runs = sorted((_e2e_call(lib, g, v["mask"], v["phi"], args.steps, dist) for _ in range(args.e2e_calls)),
+                      key=lambda x: x["wall"])
+        r = runs[len(runs) // 2]
         npts = g.num_gridpts
         h2d = 8 * npts * len(E2E_FROM_HOST)
         d2h = 8 * npts * 5 + 4 * npts + npts  # phi, phi_next, phi_prev, mask_w, mask_nw, labels, phi_bin
         e2e = {"value": dist.ws * nvox * r["steps"] / r["wall"], "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "inner_steps": r["steps"], "outer_iterations": r["outer"],
-               "wall_s": r["wall"], "phases_s": r["phases"],
-               "note": "one constCurvModel3d call with host arrays: uploads, inner steps, trapping, three "
-                       "reinitialisations, volume integrals, downloads; phases_s is the library's host-side "
-                       "split (device work is charged to the phase that waits for it)"}
+               "wall_s": r["wall"], "calls": len(runs), "wall_s_all": [round(x["wall"], 3) for x in runs],
+               "phases_s": r["phases"],
+               "note": "one constCurvModel3d call with host arrays (the median of `calls` calls, each on "
+                       "fresh host arrays): uploads, inner steps, trapping, three reinitialisations, volume "
+                       "integrals, downloads; phases_s is the library's host-side split (device work is "
+                       "charged to the phase that waits for it)"}
 
     peaks, kind = measured_peaks()
     probe = (C.c_double * 2)()
@@ -526,6 +532,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--e2e-calls", type=int, default=3, help="timed e2e calls (the median is reported)")
     ap.add_argument("--no-cpu", dest="cpu", action="store_false")
     ap.add_argument("--cpu-nz", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=3)
