@@ -524,6 +524,68 @@ def cpu_arm(args, nz: int, steps: int, warmup: int, threads: int):
             f"workload), {steps} inner WENO5/TVD-RK3 steps after {warmup} warm-up", "cores": threads}
 
 
+def ladder_arm(threads: int):
+    """Time to solution of the reference's own CPU-sized workload: the 64^3
+    drainage ladder (overlapping pack, seed 0, radius 5, porosity 0.35; ENO2 +
+    TVD-RK2, contact angle 0; curvature 0.05 -> 0.4 per voxel in 10 steps),
+    one drain_model3d call with host arrays and its per-step files, through
+    the GB300 library (z-slabs = the host's threads) and through the CPU
+    oracle on the same number of OpenMP threads.  The CFL step depends on the
+    slab split, so both runs do the same steps; their files must be equal."""
+    import gzip
+
+    lib = Q.load(Q.GPU_LIB)
+    olib = Q.load(os.path.join(ROOT, "oracle", "liboracle.so"))
+    n = 64
+    mask = S.overlapping(n, radius_vox=5.0, porosity=0.35, seed=0).mask()
+    phi = S.initial_phi(mask, n)
+    da = 0.97222
+
+    def run(l, set_par):
+        g = Q.make_grid(l, n)
+        v = Q.Volume(g)
+        v["mask"][...] = mask
+        v["phi"][...] = phi
+        o = Q.default_options(l)
+        o.theta = 0.0
+        o.order_space_accur, o.order_time_accur = 2, 2
+        o.a, o.b, o.dc = 1.25, 0.04, da / 0.04
+        o.amax, o.amin = 10.0 + 0.5 * da, 0.5
+        o.tmax, o.tplot = 0.1, 0.0167
+        o.check_connectivity = 1
+        set_par(threads)
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as d:
+            os.chdir(d)
+            try:
+                fp = Q.libc_fopen("out")
+                t0 = time.perf_counter()
+                l.drain_model3d(C.byref(o), C.byref(v.p), C.byref(g), fp)
+                t = time.perf_counter() - t0
+                Q.libc_fclose(fp)
+                files = {}
+                for f in sorted(os.listdir(d)):
+                    if f.startswith("data_step"):
+                        with gzip.open(f, "rb") as fh:
+                            files[f] = fh.read()
+            finally:
+                os.chdir(cwd)
+                set_par(1)
+        return t, files
+
+    run(lib, lib.qssgpu_set_slabs)  # warm-up: loads the kernels of every phase
+    Q.check(lib)
+    t_gpu, f_gpu = run(lib, lib.qssgpu_set_slabs)
+    Q.check(lib)
+    t_cpu, f_cpu = run(olib, olib.oracle_set_threads)
+    lib.qssgpu_set_slabs(0)
+    return {"workload": "64^3 drainage ladder (overlapping pack seed 0, radius 5, porosity 0.35), ENO2 + TVD-RK2, "
+                        "contact angle 0, curvature 0.05 -> 0.4 per voxel in 10 steps, per-step files written",
+            "slabs": threads, "gpu_s": t_gpu, "cpu_s": t_cpu, "cpu_cores": threads, "cpu_kind": "port",
+            "speedup": t_cpu / t_gpu, "steps_saved": len(f_gpu),
+            "files_identical": list(f_gpu) == list(f_cpu) and all(f_gpu[k] == f_cpu[k] for k in f_cpu)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -544,6 +606,8 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=0)
     ap.add_argument("--batch-only", action="store_true", help="measure batched mode only")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint-mode measurement")
+    ap.add_argument("--no-ladder", dest="ladder", action="store_false",
+                    help="skip the 64^3 drainage-ladder time to solution (GB300 vs CPU oracle)")
     ap.add_argument("--adjoint-only", action="store_true")
     ap.add_argument("--adj-n", type=int, default=128)
     ap.add_argument("--adj-steps", type=int, default=200)
@@ -605,6 +669,8 @@ def main():
             line["batched_mode"] = batched_arm(args)
         if args.adjoint:
             line["adjoint_mode"] = adjoint_arm(args)
+        if args.ladder and args.cpu:
+            line["ladder_64_eno2"] = ladder_arm(threads)
         print(json.dumps(line))
     dist.close()
 

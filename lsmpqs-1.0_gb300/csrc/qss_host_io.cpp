@@ -20,6 +20,9 @@
 #include "../../include/lsmpqs_types.h"
 #include "qss_fortran_abi.h"
 
+// qss_gzip.cpp: gzip file of head + data deflated on all host cores
+bool qss_gzip_write(const char* path, const void* head, size_t head_len, const void* data, size_t len);
+
 extern "C" {
 void qssgpu_release(QSS_DataArrays* p);
 void signedLinearExtrapolationBCqss(double* phi, Grid* g, int idx);
@@ -326,6 +329,17 @@ void destroyQSSDataArrays(QSS_DataArrays* p) {
 }
 
 static void write_array(const void* data, size_t elem, Grid* g, char* file_name, int zip_status, bool dims) {
+  if (zip_status == GZIP) {
+    // the final state of "write file_name, gzip -f file_name": file_name.gz
+    // holds the bytes, file_name is gone (compressed on all host cores)
+    char gz[600];
+    snprintf(gz, sizeof gz, "%s.gz", file_name);
+    if (qss_gzip_write(gz, g->grid_dims_ghostbox, dims ? 3 * sizeof(int) : 0, data,
+                       elem * (size_t)g->num_gridpts)) {
+      remove(file_name);
+      return;
+    }
+  }
   FILE* fp = fopen(file_name, "w");
   if (!fp) {
     printf("\nCould not open file %s\n", file_name);
@@ -350,6 +364,15 @@ void writeDataArrayInt(int* data, Grid* grid, char* file_name, int zip_status) {
   write_array(data, sizeof(int), grid, file_name, zip_status, true);
 }
 void writeDataArrayUcharFB(unsigned char* data_fb, Grid* g, char* file_name, int zip_status) {
+  const size_t nfb = (size_t)g->grid_dims[0] * g->grid_dims[1] * g->grid_dims[2];
+  if (zip_status == GZIP) {
+    char gz[600];
+    snprintf(gz, sizeof gz, "%s.gz", file_name);
+    if (qss_gzip_write(gz, nullptr, 0, data_fb, nfb)) {
+      remove(file_name);
+      return;
+    }
+  }
   FILE* fp = fopen(file_name, "w");
   if (!fp) return;
   fwrite(data_fb, 1, (size_t)g->grid_dims[0] * g->grid_dims[1] * g->grid_dims[2], fp);

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <initializer_list>
+#include <memory>
 #include <ctime>
 #include <algorithm>
 #include <atomic>
@@ -72,6 +73,37 @@ void dev_reservoir(DevVolume& v, const Grid* g) {
   launch_box(v.stream, v.box, v.phi_extra, g->x_lo_ghostbox, g->dx, corner, side, -1);
 }
 
+// The ladder's per-step files, written while the device runs the next
+// curvature step: each step's phi is copied into one of two host buffers
+// and a host thread writes and compresses the file (the reference writes
+// synchronously, drain_model3d.c:146-153).  At most two files are in
+// flight; all are complete when the ladder returns, with the same contents.
+class StepWriter {
+ public:
+  ~StepWriter() { join(); }
+  void write(DevVolume& v, const Grid* g, const char* name) {
+    const int b = next_;
+    next_ ^= 1;
+    if (th_[b].joinable()) th_[b].join();
+    if (!buf_[b]) buf_[b].reset(new double[(size_t)v.n]);
+    QSS_CK(cudaMemcpyAsync(buf_[b].get(), v.phi, (size_t)v.n * sizeof(double), cudaMemcpyDeviceToHost, v.stream));
+    QSS_CK(cudaStreamSynchronize(v.stream));
+    Grid gc = *g;
+    std::string nm(name);
+    double* data = buf_[b].get();
+    th_[b] = std::thread([gc, nm, data]() mutable { writeDataArrayQSS(data, &gc, &nm[0], GZIP); });
+  }
+  void join() {
+    for (auto& t : th_)
+      if (t.joinable()) t.join();
+  }
+
+ private:
+  std::unique_ptr<double[]> buf_[2];
+  std::thread th_[2];
+  int next_ = 0;
+};
+
 // The per-step files are named prefix + "data_step_<k>" (the reference's
 // names for prefix ""); a null prefix writes none.
 void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out, bool outermost,
@@ -93,6 +125,7 @@ void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out
                             H_MASK_Y, H_MASK_Z, H_CONN, H_BIN});
   }
   PrefaultGuard pg{v};
+  StepWriter files;
   char fname[256];
   int dims[3];
   double a0 = o->a;
@@ -161,12 +194,11 @@ void dev_ladder(bool drain, Options* o, QSS_DataArrays* p, Grid* g, FILE* fp_out
     v.dirty[H_PHI] = true;
     if (prefix) {
       snprintf(fname, sizeof fname, "%sdata_step_%d", prefix, step);
-      QSS_CK(cudaMemcpyAsync(p->phi, v.phi, n * sizeof(double), cudaMemcpyDeviceToHost, v.stream));
-      QSS_CK(cudaStreamSynchronize(v.stream));
-      writeDataArrayQSS(p->phi, g, fname, GZIP);
+      files.write(v, g, fname);
     }
     step += 1;
   }
+  files.join();
   if (outermost) download_dirty(v, p);
 }
 

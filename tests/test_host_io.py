@@ -140,3 +140,37 @@ def test_grid_and_files(host, oracle, tmp_path, acc):
         assert np.array_equal(np.ctypeslib.as_array(back, (n,)), data)
     finally:
         os.chdir(cwd)
+
+
+def test_gzip_members_round_trip(host, tmp_path):
+    """A saved array larger than one compression chunk is written as several
+    gzip members deflated in parallel; gzip readers (Python's and the
+    library's own readDataArrayQSS) return exactly the reference layout:
+    int[3] ghost-box dims then the values."""
+    dims = (C.c_int * 3)(150, 140, 130)
+    lo = (C.c_double * 3)(0.12, 0.12, 0.12)
+    hi = (C.c_double * 3)(0.12 + 150 * 0.04, 0.12 + 140 * 0.04, 0.12 + 130 * 0.04)
+    gh = host.createGridSetGridDims(3, dims, lo, hi, 1)
+    g = gh[0]
+    n = g.num_gridpts
+    assert n * 8 > (16 << 20)  # at least two data members
+    data = np.random.default_rng(5).standard_normal(n)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        (tmp_path / "big").write_bytes(b"stale")  # the reference's gzip -f leaves no raw file behind
+        host.writeDataArrayQSS.argtypes = [Q.c_double_p, C.POINTER(Q.Grid), C.c_char_p, C.c_int]
+        host.writeDataArrayQSS(Q.dptr(data), gh, b"big", 1)
+        assert not os.path.exists("big") and os.path.exists("big.gz")
+        with gzip.open("big.gz", "rb") as fh:
+            raw = fh.read()
+        assert list(np.frombuffer(raw[:12], dtype=np.int32)) == list(g.grid_dims_ghostbox)
+        assert np.array_equal(np.frombuffer(raw[12:], dtype=np.float64), data)
+        rd = host.readDataArrayQSS
+        rd.restype = Q.c_double_p
+        rd.argtypes = [C.POINTER(C.c_int), C.c_char_p]
+        d3 = (C.c_int * 3)()
+        back = rd(d3, b"big.gz")
+        assert np.array_equal(np.ctypeslib.as_array(back, (n,)), data)
+    finally:
+        os.chdir(cwd)
