@@ -372,7 +372,8 @@ QSS_EMU_HD double add(double x, double y) {
   return QSS_EMU_FALLBACK(2, x + y);
 }
 
-QSS_EMU_HD double sub(double x, double y) { return add(x, from_bits(bits(y) ^ kSign)); }
+QSS_EMU_HD double neg(double x);
+QSS_EMU_HD double sub(double x, double y) { return add(x, neg(y)); }
 
 // x * 2^k for a small integer k (exact unless the result leaves the normal range)
 QSS_EMU_HD double scale2(double x, int k) {
