@@ -118,19 +118,19 @@ __device__ __forceinline__ Centre make_centre(const Face& a, const Face& b, cons
   const double t2 = Q::s2(b.v, 1), t4 = Q::s2(b.v, 2);
   double t;
   t = (d.v - t2) + a.v;
-  const double A = k1312 * (t * t);
+  const double A = k1312 * Q::mul2(t, t);
   t = (a.v - t2) + d.v;
-  const double B = k1312 * (t * t);
+  const double B = k1312 * Q::mul2(t, t);
   t = (d.v - t4) + a.t3;
-  const double Cp = Q::s2(t * t, -2);
+  const double Cp = Q::s2(Q::mul2(t, t), -2);
   t = (d.t3 - t4) + a.v;
-  const double Dp = Q::s2(t * t, -2);
+  const double Dp = Q::s2(Q::mul2(t, t), -2);
   t = (a.v - t4) + d.t3;
-  const double Cm = Q::s2(t * t, -2);
+  const double Cm = Q::s2(Q::mul2(t, t), -2);
   t = (a.t3 - t4) + d.v;
-  const double Dm = Q::s2(t * t, -2);
+  const double Dm = Q::s2(Q::mul2(t, t), -2);
   t = d.v - a.v;
-  const double E = Q::s2(t * t, -2);
+  const double E = Q::s2(Q::mul2(t, t), -2);
   Centre c;
   c.s1p = A + Cp;
   c.s2p = A + E;
@@ -155,11 +155,11 @@ __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, 
   using Q = Ar<EMU>;
   double t, a1, a2, a3;
   t = S1 + eps;
-  a1 = Q::div(0.1, t * t);
+  a1 = Q::div(0.1, Q::mul2(t, t));
   t = S2 + eps;
-  a2 = Q::div(0.6, t * t);
+  a2 = Q::div(0.6, Q::mul2(t, t));
   t = S3 + eps;
-  a3 = Q::div(0.3, t * t);
+  a3 = Q::div(0.3, Q::mul2(t, t));
   const double inv_sum_a = Q::div(1.0, a1 + a2 + a3);
   a1 = Q::mul2(a1, inv_sum_a);
   a2 = Q::mul2(a2, inv_sum_a);
