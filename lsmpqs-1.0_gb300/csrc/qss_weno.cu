@@ -118,9 +118,9 @@ __device__ __forceinline__ Centre make_centre(const Face& a, const Face& b, cons
   const double t2 = Q::s2(b.v, 1), t4 = Q::s2(b.v, 2);
   double t;
   t = (d.v - t2) + a.v;
-  const double A = k1312 * Q::mul2(t, t);
+  const double A = Q::mul2(k1312, Q::mul2(t, t));
   t = (a.v - t2) + d.v;
-  const double B = k1312 * Q::mul2(t, t);
+  const double B = Q::mul2(k1312, Q::mul2(t, t));
   t = (d.v - t4) + a.t3;
   const double Cp = Q::s2(Q::mul2(t, t), -2);
   t = (d.t3 - t4) + a.v;
