@@ -26,6 +26,7 @@ std::unordered_map<const QSS_DataArrays*, DevVolume*> g_table;
 int g_slabs_override = 0;
 int g_weno_split = -1;  // -1: from the environment
 int g_emu_level = -1;   // -1: from the environment
+int g_axis_variant = -1;  // -1: from the environment, else by launch size
 }  // namespace
 
 // MADV_POPULATE_WRITE (Linux 5.14); older headers lack the name
@@ -144,6 +145,15 @@ int weno_mode() {
     m = e ? atoi(e) : 1;
   }
   return m <= 0 ? 0 : 1;
+}
+
+int axis_variant() {
+  int m = g_axis_variant;
+  if (m < 0) {
+    const char* e = getenv("QSSGPU_AXIS_VARIANT");
+    m = e ? atoi(e) : -1;
+  }
+  return m < 0 ? -1 : (m ? 1 : 0);
 }
 
 int emu_level() {
@@ -416,6 +426,12 @@ void qssgpu_set_slabs(int nslabs) { g_slabs_override = nslabs; }
 int qssgpu_set_emu_level(int level) {
   const int prev = emu_level();
   g_emu_level = level < 0 ? -1 : (level > 2 ? 2 : level);
+  return prev;
+}
+
+int qssgpu_set_axis_variant(int v) {
+  const int prev = axis_variant();
+  g_axis_variant = v < 0 ? -1 : (v ? 1 : 0);
   return prev;
 }
 

@@ -110,10 +110,11 @@ def test_const_curv_model(gpu, oracle, theta, space, time):
     assert diff_arrays(vg, vo) == {}
 
 
-@pytest.mark.parametrize("split,emu", [(0, 2), (1, 0), (1, 1), (1, 2)])
-def test_const_curv_model_weno_modes(gpu, oracle, split, emu):
+@pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 1), (1, 2, 0), (1, 2, 1)])
+def test_const_curv_model_weno_modes(gpu, oracle, split, emu, variant):
     """WENO5 + TVD-RK3 with variable coefficients through the fused stage
-    kernel and through the axis passes + combine: both equal the oracle."""
+    kernel and through the axis passes (both forms) + combine: all equal the
+    oracle."""
     g, v = pack_case(oracle, 22, seed=4)
     o_g = options(gpu, 40, 5, 3, tmax=0.02, tplot=0.01)
     o_o = options(oracle, 40, 5, 3, tmax=0.02, tplot=0.01)
@@ -123,11 +124,13 @@ def test_const_curv_model_weno_modes(gpu, oracle, split, emu):
     gpu.setSpaceDerivFunc(C.byref(g), C.byref(o_g))
     prev = gpu.qssgpu_set_weno_split(split)
     prev_emu = gpu.qssgpu_set_emu_level(emu)
+    prev_var = gpu.qssgpu_set_axis_variant(variant)
     try:
         tg = _model(gpu, vg, o_g, True, 1.25)
     finally:
         gpu.qssgpu_set_weno_split(prev)
         gpu.qssgpu_set_emu_level(prev_emu)
+        gpu.qssgpu_set_axis_variant(prev_var)
     to = _model(oracle, vo, o_o, True, 1.25)
     Q.check(gpu)
     assert tg == to
