@@ -454,7 +454,7 @@ __device__ __forceinline__ double reinit_rhs_e(const double* __restrict__ phi, c
     }
     const uint64_t acc = bits(cc) & kAbs;
     if (acc > tol_bits && acc <= 0x7ff0000000000000ull) {  // fabs(cc) > 1e-5
-      const double ngps = gs[0] * gs[0] + gs[1] * gs[1] + gs[2] * gs[2];
+      const double ngps = scale(gs[0], gs[0]) + scale(gs[1], gs[1]) + scale(gs[2], gs[2]);
       const double s = qss_emu::sqrt(ngps);
       if (!sgn_nz) return sgn - sgn * s;
       return sgn - (sgn_neg ? qss_emu::neg(s) : s);
@@ -478,7 +478,7 @@ __global__ void k_reinit_step(Box b, const double* __restrict__ data, const doub
   const int64_t c = b.idx(i, j, k);
   const double r = EMU == 0 ? reinit_rhs_at(data, phi0, distance0, b, c, inv, max_dx)
                             : reinit_rhs_e<EMU>(data, phi0, distance0, b, c, inv, max_dx, far_bits);
-  next[c] = rhs_only ? r : data[c] + dt_r * r;
+  next[c] = rhs_only ? r : data[c] + (EMU >= 2 ? qss_emu::mul(dt_r, r) : dt_r * r);
 }
 
 // ---------------------------------------------------------------------------
