@@ -327,13 +327,16 @@ __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
       const double S3 = Ap_ + 0.25 * (b3t * b3t);
       const double r1 = qss_emu::div(1.0, S1 + eps), r2 = qss_emu::div(1.0, S2 + eps),
                    r3 = qss_emu::div(1.0, S3 + eps);
-      const double q1 = r1 * r1, q2 = r2 * r2, q3 = r3 * r3;
-      const double am2 = 0.6 * q2;
-      const double am1 = 0.1 * q1, am3 = 0.3 * q3;  // minus: 0.1, 0.6, 0.3
-      const double ap1 = 0.3 * q1, ap3 = 0.1 * q3;  // plus (on S1, S2, S3): 0.3, 0.6, 0.1
+      // products of the weights on the integer pipes (the FP64 pipe bounds
+      // this kernel, its integer pipes are ~90 % idle)
+      using qss_emu::mul;
+      const double q1 = mul(r1, r1), q2 = mul(r2, r2), q3 = mul(r3, r3);
+      const double am2 = mul(0.6, q2);
+      const double am1 = mul(0.1, q1), am3 = mul(0.3, q3);  // minus: 0.1, 0.6, 0.3
+      const double ap1 = mul(0.3, q1), ap3 = mul(0.1, q3);  // plus (on S1, S2, S3): 0.3, 0.6, 0.1
       const double iam = qss_emu::div(1.0, am1 + am2 + am3), iap = qss_emu::div(1.0, ap1 + am2 + ap3);
-      const double wm1 = am1 * iam, wm2 = am2 * iam, wm3 = am3 * iam;
-      const double wp1 = ap1 * iap, wp2 = am2 * iap, wp3 = ap3 * iap;
+      const double wm1 = mul(am1, iam), wm2 = mul(am2, iam), wm3 = mul(am3, iam);
+      const double wp1 = mul(ap1, iap), wp2 = mul(am2, iap), wp3 = mul(ap3, iap);
       // candidate stencils: minus reads u0..u4, plus reads u4..u0
       const double pm1 = kC13 * u0 - kC76 * u1 + kC116 * u2;
       const double pm2 = -kC16 * u1 + kC56 * u2 + kC13 * u3;
@@ -343,8 +346,8 @@ __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
       const double pq3 = kC116 * u2 - kC76 * u3 + kC13 * u4;  // on S3 (its first)
       const double vm = wm1 * pm1 + wm2 * pm2 + wm3 * pm3;
       const double vp = wp1 * pq1 + wp2 * pq2 + wp3 * pq3;
-      const double P1 = gm * wm1, P2 = gm * wm2, P3 = gm * wm3;
-      const double Q1 = gp * wp1, Q2 = gp * wp2, Q3 = gp * wp3;
+      const double P1 = mul(gm, wm1), P2 = mul(gm, wm2), P3 = mul(gm, wm3);
+      const double Q1 = mul(gp, wp1), Q2 = mul(gp, wp2), Q3 = mul(gp, wp3);
       const double x1 = qss_emu::scale2(r1, 1), x2 = qss_emu::scale2(r2, 1), x3 = qss_emu::scale2(r3, 1);
       // x_k = 2 r_k; the minus sign of d value / d T_k is folded into the differences
       const double m1 = P1 * (vm - pm1) * x1, m2 = P2 * (vm - pm2) * x2, m3 = P3 * (vm - pm3) * x3;
