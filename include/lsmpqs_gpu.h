@@ -219,8 +219,9 @@ int qssgpu_set_weno_split(int mode);
 int qssgpu_set_emu_level(int level);
 /* form of the WENO5 axis passes at levels >= 1: 0 sliding window in
    registers, 1 the faces' scaled copies in shared memory and the smoothness
-   squares on the integer pipes, -1 the default (1, the faster form at every
-   size measured); identical results; returns the previous setting */
+   squares on the integer pipes, -1 (default) chosen by the size of the
+   launch (the second form from ~12 M fill voxels); identical results;
+   returns the previous setting */
 int qssgpu_set_axis_variant(int variant);
 /* Batched mode (no reference counterpart): the curvature ladder of
    drain_model3d (drain != 0) or imbibe_model3d on n independent volumes at

@@ -79,8 +79,9 @@ void launch_stage(cudaStream_t s, int scheme, bool var, int stage, bool final_st
 int emu_level();
 // form of the WENO5 axis passes at integer-pipe levels >= 1: 0 the sliding
 // window in registers, 1 the faces' scaled copies in shared memory with the
-// smoothness squares on the integer pipes (the default, -1, is 1;
-// $QSSGPU_AXIS_VARIANT, qssgpu_set_axis_variant); both give identical results
+// smoothness squares on the integer pipes (faster from ~12 M fill voxels),
+// -1 (default) chosen by the launch's size ($QSSGPU_AXIS_VARIANT,
+// qssgpu_set_axis_variant); both give identical results
 int axis_variant();
 
 // WENO5 variable-coefficient stage as three axis passes (one-sided

@@ -184,7 +184,7 @@ struct AxisArgs {
 // One thread: SEG consecutive voxels along axis AX starting at s0, inside
 // the fill box of that axis.  Faces s0-2 .. s0+SEG+2, centres s0-1 .. s0+SEG.
 template <int AX, int EMU, bool RING>
-__global__ void __launch_bounds__(128, RING ? 5 : 1) k_weno_axis(AxisArgs a) {
+__global__ void __launch_bounds__(128, RING ? 5 : 4) k_weno_axis(AxisArgs a) {
   if (a.ctl && !a.ctl->active) return;
   const Box& b = a.b;
   // lanes run along i for the y and z passes (coalesced); for the x pass they
@@ -247,15 +247,22 @@ __global__ void __launch_bounds__(128, RING ? 5 : 1) k_weno_axis(AxisArgs a) {
   // barrier): the sliding window then holds ~30 fewer registers per thread
   // and more warps stay resident.  Face r of the segment (r = m - s0 + 2)
   // uses slot r mod 6.
-  __shared__ double ring[RING ? 6 : 1][5][RING ? 128 : 1];
+  // (the register form declares no shared memory: its x pass streams rows
+  // through L1, which a shared-memory carve-out would shrink)
+  double* ring = nullptr;
+  if constexpr (RING) {
+    __shared__ double ring_mem[6 * 5 * 128];
+    ring = ring_mem;
+  }
   const int tx = RING ? threadIdx.x : 0;
+  auto R = [&](int slot, int k) -> double& { return ring[(slot * 5 + k) * 128 + tx]; };
   auto put = [&](int slot, const Face& f) {
     if (!RING) return;
-    ring[slot][0][tx] = f.c13;
-    ring[slot][1][tx] = f.c76;
-    ring[slot][2][tx] = f.c116;
-    ring[slot][3][tx] = f.c16;
-    ring[slot][4][tx] = f.c56;
+    R(slot, 0) = f.c13;
+    R(slot, 1) = f.c76;
+    R(slot, 2) = f.c116;
+    R(slot, 3) = f.c16;
+    R(slot, 4) = f.c56;
   };
   int sm2 = 0, sm1 = 1, sz = 2, sp1 = 3, sp2 = 4, sp3 = 5;
   put(sm2, fm2);
@@ -279,17 +286,17 @@ __global__ void __launch_bounds__(128, RING ? 5 : 1) k_weno_axis(AxisArgs a) {
       // the scaled copies of faces i-2 .. i+2
       double c13m2, c76m1, c16m1, c13z, c116z, c56z, c13p1, c116p1, c56p1, c76p2, c16p2;
       if (RING) {
-        c13m2 = ring[sm2][0][tx];
-        c76m1 = ring[sm1][1][tx];
-        c16m1 = ring[sm1][3][tx];
-        c13z = ring[sz][0][tx];
-        c116z = ring[sz][2][tx];
-        c56z = ring[sz][4][tx];
-        c13p1 = ring[sp1][0][tx];
-        c116p1 = ring[sp1][2][tx];
-        c56p1 = ring[sp1][4][tx];
-        c76p2 = ring[sp2][1][tx];
-        c16p2 = ring[sp2][3][tx];
+        c13m2 = R(sm2, 0);
+        c76m1 = R(sm1, 1);
+        c16m1 = R(sm1, 3);
+        c13z = R(sz, 0);
+        c116z = R(sz, 2);
+        c56z = R(sz, 4);
+        c13p1 = R(sp1, 0);
+        c116p1 = R(sp1, 2);
+        c56p1 = R(sp1, 4);
+        c76p2 = R(sp2, 1);
+        c16p2 = R(sp2, 3);
       } else {
         c13m2 = fm2.c13;
         c76m1 = fm1.c76;
@@ -502,6 +509,8 @@ __global__ void __launch_bounds__(128) k_weno_combine(CombineArgs a) {
   if (FINAL) a.phi_new[idx] = impose3_e<EMU>(out, idx, a.im);
 }
 
+constexpr int64_t kRingVoxels = 12LL << 20;
+
 template <int EMU>
 void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[3], double* const dp[3],
              double* const dm[3], const Ctl* ctl) {
@@ -524,9 +533,11 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     }
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
     dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
-    // the shared-memory form is the faster one at every size measured on
-    // GB300 (128^3: 385 against 362 M voxel-steps/s, 512^3: 488 against 454)
-    const int var = axis_variant() == 0 ? 0 : 1;
+    // the shared-memory form is the faster one from ~12 M fill voxels on
+    // (measured on GB300, register / shared-memory form, M voxel-steps/s:
+    // 128^3 420 / 383, 192^3 400 / 385, 256^3 458 / 473, 512^3 469 / 488)
+    int var = axis_variant();
+    if (var < 0) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
     cudaEvent_t e0 = ctl ? prof_open(s) : nullptr;
     if (EMU == 0 || var == 0) {
       if (ax == 0) k_weno_axis<0, EMU, false><<<g, 128, 0, s>>>(a);
