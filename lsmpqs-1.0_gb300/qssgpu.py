@@ -247,20 +247,22 @@ class Volume:
     """All arrays of one ``QSS_DataArrays`` as numpy buffers (ghost box,
     column-major: numpy shape (nz, ny, nx))."""
 
-    def __init__(self, g: Grid):
+    def __init__(self, g: Grid, alloc=None):
+        """alloc(shape, dtype) -> zeroed ndarray overrides np.zeros (e.g. page-locked buffers)."""
         self.g = g
         nx, ny, nz = (g.grid_dims_ghostbox[d] for d in range(3))
         self.shape = (nz, ny, nx)
         self.arrays: dict[str, np.ndarray] = {}
         self.p = QSSDataArrays()
+        zeros = alloc or (lambda shape, dtype: np.zeros(shape, dtype=dtype))
         for name in REAL_ARRAYS + REAL_ARRAYS_2:
-            a = np.zeros(self.shape, dtype=np.float64)
+            a = zeros(self.shape, np.float64)
             self.arrays[name] = a
             setattr(self.p, name, a.ctypes.data_as(c_double_p))
-        a = np.zeros(self.shape, dtype=np.int32)
+        a = zeros(self.shape, np.int32)
         self.arrays["connectivity"] = a
         self.p.connectivity = a.ctypes.data_as(c_int_p)
-        a = np.zeros(self.shape, dtype=np.uint8)
+        a = zeros(self.shape, np.uint8)
         self.arrays["phi_bin"] = a
         self.p.phi_bin = a.ctypes.data_as(c_uchar_p)
 
