@@ -518,13 +518,19 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     const int along = ax == 0 ? b.fbx() : (ax == 1 ? b.fby() : b.fbz());
     const int lanes = ax == 0 ? b.fby() : b.fbx();
     const int other = ax == 2 ? b.fby() : b.fbz();
+    // the shared-memory form is the faster one from ~12 M fill voxels on
+    // (measured on GB300, register / shared-memory form, M voxel-steps/s:
+    // 128^3 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
+    int var = axis_variant();
+    if (var < 0) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
     // a segment recomputes 5 faces and 3 centres before its first voxel:
-    // segments as long as the line allows while the launch still fills
-    // about four waves of 12 warps on every SM (at least SEG voxels)
+    // segments as long as the line allows while the launch still fills about
+    // eight (register form) or four (shared-memory form) waves of 12 warps on
+    // every SM, and at least SEG voxels
     int len = SEG;
     if (EMU != 0) {
       const int64_t lines = (int64_t)lanes * other;
-      const int64_t want = 4LL * 152 * 12 * 32;
+      const int64_t want = (var ? 4LL : 8LL) * 152 * 12 * 32;
       int64_t nseg = (want + lines - 1) / lines;
       const int64_t most = (along + SEG - 1) / SEG;
       if (nseg > most) nseg = most;
@@ -533,11 +539,6 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     }
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
     dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
-    // the shared-memory form is the faster one from ~12 M fill voxels on
-    // (measured on GB300, register / shared-memory form, M voxel-steps/s:
-    // 128^3 420 / 383, 192^3 400 / 385, 256^3 458 / 473, 512^3 469 / 488)
-    int var = axis_variant();
-    if (var < 0) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
     cudaEvent_t e0 = ctl ? prof_open(s) : nullptr;
     if (EMU == 0 || var == 0) {
       if (ax == 0) k_weno_axis<0, EMU, false><<<g, 128, 0, s>>>(a);
