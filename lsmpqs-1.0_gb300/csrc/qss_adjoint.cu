@@ -631,6 +631,28 @@ struct StageDerivs {
   double* d[3][6] = {};  // [stage][dp x, y, z, dm x, y, z]
 };
 
+// the stage states (and, when device memory allows, the stage inputs' WENO5
+// derivatives) of the steps of one checkpoint segment
+struct SegBufs {
+  std::vector<double*> sphi, ss1, ss2, ss3;
+  std::vector<StageDerivs> sder;
+  void alloc(DBufs& buf, int steps, int64_t n, bool derivs) {
+    for (int q = 0; q < steps; q++) {
+      sphi.push_back(buf.get(n));
+      ss1.push_back(buf.get(n));
+      ss2.push_back(buf.get(n));
+      ss3.push_back(buf.get(n));
+    }
+    if (derivs) {
+      sder.resize(steps);
+      for (auto& sd : sder)
+        for (int st = 0; st < 3; st++)
+          for (int c = 0; c < 6; c++) sd.d[st][c] = buf.get(n);
+    }
+  }
+  const StageDerivs* keep(int q) const { return sder.empty() ? nullptr : &sder[q]; }
+};
+
 // one forward step from phin: stage states s1, s2, s3 (ghosts valid) and
 // phi^{n+1}; with keep, the stage inputs' WENO5 derivatives stay in *keep
 void fwd_step(AdjCtx& a, const double* phin, double* s1, double* s2, double* s3, double* next,
@@ -731,25 +753,22 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
     // buffers hold the stage states of one segment (the last one straight
     // from this forward pass, the others recomputed in the backward pass)
     std::vector<double*> cp(nseg, nullptr);
-    std::vector<double*> sphi, ss1, ss2, ss3;
-    std::vector<StageDerivs> sder;  // per segment step, when device memory allows
+    // segment buffers; with two sets (when device memory allows) segment k-1
+    // is recomputed on a second stream while the reverse sweep runs over
+    // segment k
+    SegBufs sets[2];
+    int nsets = 0;
     if (want_grad) {
       for (int k = 0; k < nseg - 1; k++) cp[k] = buf.get(n);
-      for (int q = 0; q < ckpt; q++) {
-        sphi.push_back(buf.get(n));
-        ss1.push_back(buf.get(n));
-        ss2.push_back(buf.get(n));
-        ss3.push_back(buf.get(n));
-      }
       size_t free_b = 0, total_b = 0;
       QSS_CK(cudaMemGetInfo(&free_b, &total_b));
-      const double need = (double)ckpt * 18 * bytes + (double)(15 + 8) * bytes;
-      if (need < 0.6 * (double)free_b) {
-        sder.resize(ckpt);
-        for (auto& sd : sder)
-          for (int st = 0; st < 3; st++)
-            for (int c = 0; c < 6; c++) sd.d[st][c] = buf.get(n);
-      }
+      const double per_set = (double)ckpt * (4 + 18) * bytes;
+      const double rest = (double)(15 + 8) * bytes;
+      const bool derivs = per_set + rest < 0.6 * (double)free_b;
+      // (two sets need the kept derivatives: without them both streams
+      // would share the derivative scratch)
+      nsets = (derivs && nseg > 1 && 2 * per_set + rest < 0.6 * (double)free_b) ? 2 : 1;
+      for (int k = 0; k < nsets; k++) sets[k].alloc(buf, ckpt, n, derivs);
     }
     double* cur = buf.get(n);
     double* nxt = buf.get(n);
@@ -761,10 +780,11 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
       if (want_grad && st % ckpt == 0 && st < last0)
         QSS_CK(cudaMemcpyAsync(cp[st / ckpt], cur, bytes, cudaMemcpyDeviceToDevice, a.s));
       if (want_grad && st >= last0) {
+        SegBufs& sb = sets[(nseg - 1) % nsets];
         const int q = st - last0;
-        if (q == 0) QSS_CK(cudaMemcpyAsync(sphi[0], cur, bytes, cudaMemcpyDeviceToDevice, a.s));
-        double* next = (st + 1 < nsteps) ? sphi[q + 1] : nxt;
-        fwd_step(a, sphi[q], ss1[q], ss2[q], ss3[q], next, sder.empty() ? nullptr : &sder[q]);
+        if (q == 0) QSS_CK(cudaMemcpyAsync(sb.sphi[0], cur, bytes, cudaMemcpyDeviceToDevice, a.s));
+        double* next = (st + 1 < nsteps) ? sb.sphi[q + 1] : nxt;
+        fwd_step(a, sb.sphi[q], sb.ss1[q], sb.ss2[q], sb.ss3[q], next, sb.keep(q));
         cur = next;
       } else {
         fwd_step(a, cur, t1, t2, t3, nxt);
@@ -891,39 +911,76 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
       k_adj_axis<2><<<ag2, 128, 0, a.s>>>(ax);
       k_adj_curv<<<g1(n), 256, 0, a.s>>>(b, cc, n, lam_in, coef_id, lam_out);
     };
+    // recomputation of segment k's states from its checkpoint, on stream st
+    AdjCtx a2 = a;
+    cudaStream_t s2 = a.s;
+    if (nsets == 2) QSS_CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    a2.s = s2;
+    cudaEvent_t recomputed[2] = {}, released[2] = {};
+    for (int k = 0; k < 2; k++) {
+      QSS_CK(cudaEventCreateWithFlags(&recomputed[k], cudaEventDisableTiming));
+      QSS_CK(cudaEventCreateWithFlags(&released[k], cudaEventDisableTiming));
+    }
+    auto recompute = [&](int k) {
+      SegBufs& sb = sets[k % nsets];
+      AdjCtx& c = (nsets == 2) ? a2 : a;
+      const int s0 = k * ckpt, s1 = std::min(nsteps, s0 + ckpt);
+      QSS_CK(cudaMemcpyAsync(sb.sphi[0], cp[k], bytes, cudaMemcpyDeviceToDevice, c.s));
+      for (int st = s0; st < s1; st++) {
+        const int q = st - s0;
+        double* next = (q + 1 < s1 - s0) ? sb.sphi[q + 1] : t1;
+        fwd_step(c, sb.sphi[q], sb.ss1[q], sb.ss2[q], sb.ss3[q], next, sb.keep(q));
+      }
+      QSS_CK(cudaEventRecord(recomputed[k % 2], c.s));
+    };
+    if (nsets == 2 && nseg >= 2) {
+      // the checkpoints and coefficients come from work queued on a.s
+      QSS_CK(cudaEventRecord(released[(nseg - 1) % 2], a.s));
+      QSS_CK(cudaStreamWaitEvent(s2, released[(nseg - 1) % 2], 0));
+      recompute(nseg - 2);
+    }
     for (int k = nseg - 1; k >= 0; k--) {
       const int s0 = k * ckpt, s1 = std::min(nsteps, s0 + ckpt);
-      // recompute the segment's states (the last segment's are still there)
+      SegBufs& sb = sets[k % nsets];
       if (k < nseg - 1) {
-        QSS_CK(cudaMemcpyAsync(sphi[0], cp[k], bytes, cudaMemcpyDeviceToDevice, a.s));
-        for (int st = s0; st < s1; st++) {
-          const int q = st - s0;
-          double* next = (q + 1 < s1 - s0) ? sphi[q + 1] : t1;
-          fwd_step(a, sphi[q], ss1[q], ss2[q], ss3[q], next, sder.empty() ? nullptr : &sder[q]);
-        }
+        if (nsets == 2) QSS_CK(cudaStreamWaitEvent(a.s, recomputed[k % 2], 0));
+        else recompute(k);
+      }
+      // the set of segment k-1 is the one the reverse sweep of segment k+1
+      // has released: recompute it now, beside the sweep over segment k
+      if (nsets == 2 && k >= 1 && k - 1 < nseg - 2) {
+        QSS_CK(cudaStreamWaitEvent(s2, released[(k + 1) % 2], 0));
+        recompute(k - 1);
       }
       for (int st = s1 - 1; st >= s0; st--) {
         const int q = st - s0;
         // phi^{n+1} = impose(BC(s3))
-        k_adj_impose<<<g1(n), 256, 0, a.s>>>(n, ss3[q], mask, o->overlap, lam, lam3);
-        bc_bwd(ss3[q], lam3);
+        k_adj_impose<<<g1(n), 256, 0, a.s>>>(n, sb.ss3[q], mask, o->overlap, lam, lam3);
+        bc_bwd(sb.ss3[q], lam3);
         // stage 3: s3 = 1/3 phi^n + 2/3 (s2 + dt L(s2))
         launch_fill(a.s, n, lamphi, 0.0);
         launch_fill(a.s, n, lam2, 0.0);
-        const StageDerivs* sd = sder.empty() ? nullptr : &sder[q];
-        stage_bwd(ss2[q], lam3, 2.0 / 3.0, 2.0 / 3.0 * dt, lam2, sd, 2);
+        const StageDerivs* sd = sb.keep(q);
+        stage_bwd(sb.ss2[q], lam3, 2.0 / 3.0, 2.0 / 3.0 * dt, lam2, sd, 2);
         k_axpy_fill<<<g1(n), 256, 0, a.s>>>(b, lam3, 1.0 / 3.0, lamphi);
-        bc_bwd(ss2[q], lam2);
+        bc_bwd(sb.ss2[q], lam2);
         // stage 2: s2 = 3/4 phi^n + 1/4 (s1 + dt L(s1))
         launch_fill(a.s, n, lam1, 0.0);
-        stage_bwd(ss1[q], lam2, 0.25, 0.25 * dt, lam1, sd, 1);
+        stage_bwd(sb.ss1[q], lam2, 0.25, 0.25 * dt, lam1, sd, 1);
         k_axpy_fill<<<g1(n), 256, 0, a.s>>>(b, lam2, 0.75, lamphi);
-        bc_bwd(ss1[q], lam1);
+        bc_bwd(sb.ss1[q], lam1);
         // stage 1: s1 = phi^n + dt L(phi^n)
-        stage_bwd(sphi[q], lam1, 1.0, dt, lamphi, sd, 0);
+        stage_bwd(sb.sphi[q], lam1, 1.0, dt, lamphi, sd, 0);
         std::swap(lam, lamphi);
       }
+      QSS_CK(cudaEventRecord(released[k % 2], a.s));
     }
+    QSS_CK(cudaStreamSynchronize(s2));
+    for (int k = 0; k < 2; k++) {
+      cudaEventDestroy(recomputed[k]);
+      cudaEventDestroy(released[k]);
+    }
+    if (nsets == 2) cudaStreamDestroy(s2);
     k_adj_theta<<<grd, blk, 0, a.s>>>(b, mask, mxyz[0], mxyz[1], mxyz[2], th, adj_vel, g->dx[0], gth);
     QSS_CK(cudaGetLastError());
     // gradient on the fill box, zero on the ghost layers
