@@ -8,7 +8,7 @@
 // memory.  qssgpu_volume_noalloc() serves them: it reads phi from a device
 // pointer, writes the volume to a device pointer and keeps its only
 // intermediate data -- one contribution per fill-box voxel, summed in the
-// reference's loop order -- in the fixed array below, which the driver
+// reference's loop order -- in the fixed array below, which the CUDA driver
 // creates with the library's module on every GPU that loads it and keeps
 // until the process exits.  Nothing here calls cudaMalloc, cudaFree or any
 // allocating library routine.
