@@ -621,7 +621,7 @@ def main():
     ap.add_argument("--fp64-peak", type=float, default=1.25)
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the batched-mode measurement (uneven volumes)")
-    ap.add_argument("--batch-volumes", type=int, default=16)
+    ap.add_argument("--batch-volumes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-workers", type=int, default=0)
     ap.add_argument("--batch-only", action="store_true", help="measure batched mode only")
