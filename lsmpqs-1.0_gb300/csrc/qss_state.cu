@@ -365,16 +365,10 @@ void start_prefault(DevVolume& v, const QSS_DataArrays* p, std::initializer_list
 void download_dirty(DevVolume& v, QSS_DataArrays* p) {
   PhaseTimer pt(v, PH_DOWNLOAD);
   v.prefault.join();
-  // arrays the reference leaves zero: cleared on host threads, one per array,
-  // while the copies run
-  struct Joiner {
-    std::vector<std::thread> t;
-    ~Joiner() {
-      for (auto& x : t)
-        if (x.joinable()) x.join();
-    }
-  } clear;
-  bool synced = false;
+  // arrays the reference leaves zero: copied from a zeroed device buffer (the
+  // reinitialisation scratch, free once the call's work is queued) by the
+  // copy engine, which writes host memory faster than a CPU memset
+  bool zeroed = false;
   for (int a = 0; a < H_COUNT; a++) {
     HostArray w = (HostArray)a;
     void* h = host_ptr(p, w);
@@ -383,10 +377,10 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
       continue;
     }
     if (v.zero_on_return[a]) {
-      if (!synced) QSS_CK(cudaStreamSynchronize(v.stream));
-      synced = true;
-      const size_t bytes = (size_t)v.n * elem_size(w);
-      clear.t.emplace_back([h, bytes] { memset(h, 0, bytes); });
+      const size_t bytes = (size_t)v.n * elem_size(w);  // at most n doubles
+      if (!zeroed) QSS_CK(cudaMemsetAsync(v.r_next, 0, (size_t)v.n * sizeof(double), v.stream));
+      zeroed = true;
+      QSS_CK(cudaMemcpyAsync(h, v.r_next, bytes, cudaMemcpyDeviceToHost, v.stream));
     } else if (v.dirty[a]) {
       void* d = dev_ptr(v, w);
       if (!d) continue;
@@ -407,7 +401,6 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
     }
     v.dirty[a] = v.zero_on_return[a] = false;
   }
-  for (auto& t : clear.t) t.join();
   QSS_CK(cudaStreamSynchronize(v.stream));
 }
 
