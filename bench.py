@@ -244,7 +244,7 @@ def gpu_arm(args, dist: Dist):
         e2e = {"value": dist.ws * nvox * r["steps"] / r["wall"], "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "inner_steps": r["steps"], "outer_iterations": r["outer"],
                "wall_s": r["wall"], "calls": len(runs), "wall_s_all": [round(x["wall"], 3) for x in runs],
-               "phases_s": r["phases"], "host_arrays": "page-locked (cudaHostRegister)",
+               "phases_s": r["phases"], "host_arrays": "page-locked (qssgpu_host_alloc)",
                "pageable": {"value": dist.ws * nvox * pg["steps"] / pg["wall"], "wall_s": pg["wall"],
                             "phases_s": pg["phases"]},
                "note": "one constCurvModel3d call with page-locked host arrays (the median of `calls` calls, "
@@ -288,19 +288,22 @@ PHASES = ["total", "setup", "upload", "inner", "trap", "reinit", "reduce", "down
 def _e2e_call(lib, g, mask, phi, steps, dist, pinned=False):
     """One constCurvModel3d call on fresh host arrays holding (mask, phi),
     timed on the host; returns wall time, inner steps and the phase split.
-    With pinned, the arrays are page-locked (cudaHostRegister) before the
-    timed call and released after it."""
-    w = Q.Volume(g)
+    With pinned, the arrays are page-locked host memory from the library's
+    qssgpu_host_alloc (cudaHostAlloc), freed after the call."""
+    buffers = []
+
+    def pinned_zeros(shape, dtype):
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        ptr = lib.qssgpu_host_alloc(nbytes)
+        if not ptr:
+            raise RuntimeError("qssgpu_host_alloc failed")
+        buffers.append(ptr)
+        raw = (C.c_ubyte * nbytes).from_address(ptr)
+        return np.frombuffer(raw, dtype=dtype).reshape(shape)
+
+    w = Q.Volume(g, alloc=pinned_zeros if pinned else None)
     w["mask"][...] = mask
     w["phi"][...] = phi
-    registered = []
-    if pinned:
-        import torch
-
-        rt = torch.cuda.cudart()
-        for a in w.arrays.values():
-            if rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0) == rt.cudaError.success:
-                registered.append(a)
     o = Q.default_options(lib)
     set_options(lib, o)
     _fill_host_coefficients(lib, o, w, o.a)
@@ -318,14 +321,12 @@ def _e2e_call(lib, g, mask, phi, steps, dist, pinned=False):
     ph = (C.c_double * 8)()
     lib.qssgpu_call_times(C.byref(w.p), C.byref(g), ph)
     lib.qssgpu_release(C.byref(w.p))
-    if registered:
-        import torch
-
-        rt = torch.cuda.cudart()
-        for a in registered:
-            rt.cudaHostUnregister(a.ctypes.data)
-    return {"wall": dist.max(t1 - t0), "steps": steps_done.value, "outer": outer.value,
+    res = {"wall": dist.max(t1 - t0), "steps": steps_done.value, "outer": outer.value,
             "phases": {k: round(ph[i], 3) for i, k in enumerate(PHASES) if k not in ("total", "setup")}}
+    del w
+    for ptr in buffers:
+        lib.qssgpu_host_free(ptr)
+    return res
 
 
 def _fill_host_coefficients(lib, o, w, a0):

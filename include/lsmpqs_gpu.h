@@ -305,6 +305,11 @@ int qssgpu_op_rates(double *out);
 int qssgpu_get_slabs(const Grid *g);
 /* frees the device copy kept for p (destroyQSSDataArrays calls it) */
 void qssgpu_release(QSS_DataArrays *p);
+/* page-locked, zeroed host memory for the arrays of a QSS_DataArrays (the
+   copies to and from the device then skip the driver's staging); NULL on
+   failure; release with qssgpu_host_free */
+void *qssgpu_host_alloc(size_t bytes);
+void qssgpu_host_free(void *h);
 /* inner steps and outer iterations of the last top-level call on p */
 void qssgpu_call_stats(const QSS_DataArrays *p, const Grid *g, long long *inner_steps,
                        long long *outer_iters);

@@ -438,6 +438,25 @@ int qssgpu_get_slabs(const Grid* g) { return g ? num_slabs_for(g) : g_slabs_over
 
 void qssgpu_release(QSS_DataArrays* p) { release_volume(p); }
 
+// See include/lsmpqs_gpu.h.
+void* qssgpu_host_alloc(size_t bytes) {
+  try {
+    ensure_device();
+    void* h = nullptr;
+    QSS_CK(cudaHostAlloc(&h, bytes ? bytes : 1, cudaHostAllocDefault));
+    memset(h, 0, bytes);
+    return h;
+  } catch (const Error& e) {
+    set_error(e.code, e.what());
+    return nullptr;
+  }
+}
+
+// See include/lsmpqs_gpu.h.
+void qssgpu_host_free(void* h) {
+  if (h) cudaFreeHost(h);
+}
+
 int qssgpu_device_available(void) {
   try {
     ensure_device();
