@@ -197,3 +197,39 @@ def test_drain_imbibe_ladder(gpu, oracle, theta, space, time, imbibe):
     for k in fo:
         assert fg[k] == fo[k], k
     assert diff_arrays(vg, vo) == {}
+
+
+def test_model_on_page_locked_arrays(gpu, oracle):
+    """constCurvModel3d on arrays from qssgpu_host_alloc (page-locked: the
+    uploads run asynchronously) equals the oracle on ordinary arrays."""
+    g, v = pack_case(oracle, 20, seed=8)
+    ptrs = []
+
+    def pinned(shape, dtype):
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        ptr = gpu.qssgpu_host_alloc(nbytes)
+        assert ptr
+        ptrs.append(ptr)
+        raw = (C.c_ubyte * nbytes).from_address(ptr)
+        return np.frombuffer(raw, dtype=dtype).reshape(shape)
+
+    vg = Q.Volume(g, alloc=pinned)
+    assert all(not a.any() for a in vg.arrays.values())  # zeroed
+    vg.copy_from(v)
+    vo = clone(v)
+    o_g = options(gpu, 30, 5, 3, tmax=0.02, tplot=0.01)
+    o_o = options(oracle, 30, 5, 3, tmax=0.02, tplot=0.01)
+    prepare_model(oracle, o_g, vg, 1.25)
+    prepare_model(oracle, o_o, vo, 1.25)
+    gpu.setSpaceDerivFunc(C.byref(g), C.byref(o_g))
+    try:
+        tg = _model(gpu, vg, o_g, True, 1.25)
+        to = _model(oracle, vo, o_o, True, 1.25)
+        Q.check(gpu)
+        assert tg == to
+        assert diff_arrays(vg, vo) == {}
+    finally:
+        gpu.qssgpu_release(C.byref(vg.p))
+        del vg
+        for p in ptrs:
+            gpu.qssgpu_host_free(p)
