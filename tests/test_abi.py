@@ -8,6 +8,7 @@ import re
 import subprocess
 import tempfile
 
+import numpy as np
 import pytest
 
 import qssgpu as Q
@@ -80,4 +81,31 @@ def test_no_device_is_reported_not_crashed(lib):
     assert t == -1
     assert L.qssgpu_last_error() != 0
     assert b"CUDA" in L.qssgpu_error_string() or b"device" in L.qssgpu_error_string()
+    L.qssgpu_clear_error()
+
+
+def test_host_side_argument_checks(lib):
+    """Checks that run before any device work: the batch rejects volumes that
+    share arrays or options, and without a GPU the page-locked allocator and
+    the phase-image call fail cleanly with an error code."""
+    L = Q.load(Q.GPU_LIB)
+    g = Q.make_grid(L, 8)
+    v = Q.Volume(g)
+    o1, o2 = Q.default_options(L), Q.default_options(L)
+    arr_o = (C.POINTER(Q.Options) * 2)(C.pointer(o1), C.pointer(o2))
+    arr_p = (C.POINTER(Q.QSSDataArrays) * 2)(C.pointer(v.p), C.pointer(v.p))  # shared arrays
+    arr_g = (C.POINTER(Q.Grid) * 2)(C.pointer(g), C.pointer(g))
+    L.qssgpu_clear_error()
+    assert L.qssgpu_ladder_batch(1, 2, arr_o, arr_p, arr_g, None, None, 0) == 2
+    assert b"share" in L.qssgpu_error_string()
+    L.qssgpu_clear_error()
+    if L.qssgpu_device_available():
+        return
+    assert not L.qssgpu_host_alloc(1 << 20)
+    assert L.qssgpu_last_error() != 0
+    L.qssgpu_clear_error()
+    full = np.zeros(v.shape, dtype=np.uint8)
+    rc = L.qssgpu_phase_uchar(Q.dptr(v["phi"]), Q.dptr(v["mask"]), C.byref(g), b"n",
+                              full.ctypes.data_as(C.POINTER(C.c_ubyte)), None)
+    assert rc != 0 and L.qssgpu_last_error() != 0
     L.qssgpu_clear_error()
