@@ -88,11 +88,7 @@ bool member(const ZLib& z, const unsigned char* p, size_t n, std::vector<unsigne
   return true;
 }
 
-}  // namespace
-
-// Writes path as gzip of head (head_len bytes) followed by data (len bytes).
-// Returns false, writing nothing, when zlib is unavailable or fails.
-bool qss_gzip_write(const char* path, const void* head, size_t head_len, const void* data, size_t len) {
+bool gzip_write(const char* path, const void* head, size_t head_len, const void* data, size_t len) {
   const ZLib& z = zlib();
   if (!z.ok) return false;
   const unsigned char* d = (const unsigned char*)data;
@@ -123,4 +119,18 @@ bool qss_gzip_write(const char* path, const void* head, size_t head_len, const v
   if (fclose(fp) != 0) good = false;
   if (!good) remove(path);
   return good;
+}
+
+}  // namespace
+
+// Writes path as gzip of head (head_len bytes) followed by data (len bytes).
+// Returns false, writing nothing, when zlib is unavailable or fails (the
+// caller then writes the file and runs the gzip program, as the reference).
+bool qss_gzip_write(const char* path, const void* head, size_t head_len, const void* data, size_t len) {
+  try {
+    return gzip_write(path, head, head_len, data, len);
+  } catch (...) {  // out of host memory for the compressed chunks, or no threads
+    remove(path);
+    return false;
+  }
 }
