@@ -220,9 +220,19 @@ int qssgpu_set_emu_level(int level);
 /* form of the WENO5 axis passes at levels >= 1: 0 sliding window in
    registers, 1 the faces' scaled copies in shared memory and the smoothness
    squares on the integer pipes, -1 (default) chosen by the size of the
-   launch (the second form from ~12 M fill voxels); identical results;
-   returns the previous setting */
+   launch (the second form from ~12 M fill voxels), 2 tuned: the first pass
+   over each line shape times every distinct (form, segment length) and the
+   fastest is kept for that shape (one stream synchronisation per new shape
+   and axis); identical results; returns the previous setting.  No
+   reference counterpart: the reference's getrhs3d5th_ (3d.f:1968-2138) is a
+   loop over voxels with nothing to tune. */
 int qssgpu_set_axis_variant(int variant);
+/* the launch shapes chosen in tuned mode so far: at most max_rows rows of 7
+   ints (arithmetic level, axis, lanes, lines per lane, line length, form,
+   segment length) into rows (may be NULL); returns the number of shapes */
+int qssgpu_axis_tuning(int* rows, int max_rows);
+/* forgets the tuned launch shapes */
+void qssgpu_axis_tuning_reset(void);
 /* Batched mode (no reference counterpart): the curvature ladder of
    drain_model3d (drain != 0) or imbibe_model3d on n independent volumes at
    once, each with its own Options (contact angle, curvature ladder), arrays

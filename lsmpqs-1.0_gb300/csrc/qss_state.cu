@@ -153,7 +153,7 @@ int axis_variant() {
     const char* e = getenv("QSSGPU_AXIS_VARIANT");
     m = e ? atoi(e) : -1;
   }
-  return m < 0 ? -1 : (m ? 1 : 0);
+  return m < 0 ? -1 : (m > 2 ? 2 : m);
 }
 
 int emu_level() {
@@ -424,7 +424,7 @@ int qssgpu_set_emu_level(int level) {
 
 int qssgpu_set_axis_variant(int v) {
   const int prev = axis_variant();
-  g_axis_variant = v < 0 ? -1 : (v ? 1 : 0);
+  g_axis_variant = v < 0 ? -1 : (v > 2 ? 2 : v);
   return prev;
 }
 

@@ -29,6 +29,11 @@
 //   B(c) = 13/12((v(c-1) - 2v(c)) + v(c+1))^2   first term of S1-(c+1), S2-(c), S3-(c-1)
 //   E(c) = 1/4 (v(c+1) - v(c-1))^2              second term of S2+(c-1) and S2-(c)
 //   eps-(i) = eps+(i-1)                          (same five squares, max is exact)
+#include <array>
+#include <map>
+#include <mutex>
+#include <vector>
+
 #include "qss_emu.cuh"
 #include "qss_kernels.cuh"
 
@@ -511,9 +516,91 @@ __global__ void __launch_bounds__(128) k_weno_combine(CombineArgs a) {
 
 constexpr int64_t kRingVoxels = 12LL << 20;
 
+// a segment recomputes 5 faces and 3 centres before its first voxel:
+// segments as long as the line allows while the launch still fills about
+// `waves` waves of 12 warps on every SM, and at least SEG voxels
+int seg_len_for(int64_t lines, int along, int64_t waves) {
+  const int64_t want = waves * 152 * 12 * 32;
+  int64_t nseg = (want + lines - 1) / lines;
+  const int64_t most = (along + SEG - 1) / SEG;
+  if (nseg > most) nseg = most;
+  if (nseg < 1) nseg = 1;
+  return (int)((along + nseg - 1) / nseg);
+}
+
+template <int EMU>
+void launch_axis(cudaStream_t s, int ax, int var, AxisArgs a, int lanes, int other, int along, int len) {
+  a.seg_len = len;
+  dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
+  if (EMU == 0 || var == 0) {
+    if (ax == 0) k_weno_axis<0, EMU, false><<<g, 128, 0, s>>>(a);
+    else if (ax == 1) k_weno_axis<1, EMU, false><<<g, 128, 0, s>>>(a);
+    else k_weno_axis<2, EMU, false><<<g, 128, 0, s>>>(a);
+  } else {
+    if (ax == 0) k_weno_axis<0, EMU, EMU != 0><<<g, 128, 0, s>>>(a);
+    else if (ax == 1) k_weno_axis<1, EMU, EMU != 0><<<g, 128, 0, s>>>(a);
+    else k_weno_axis<2, EMU, EMU != 0><<<g, 128, 0, s>>>(a);
+  }
+}
+
+// Tuned launch shapes (axis variant 2): per line shape (level, axis, lanes,
+// lines per lane row, line length) the form and segment length that ran
+// fastest the first time that shape was met.
+using TuneKey = std::array<int, 5>;
+std::mutex g_tune_mu;
+std::map<TuneKey, std::array<int, 2>> g_tune;
+
+// Times every distinct (form, segment length) candidate of one axis pass on
+// stream s, one launch each after one untimed launch, and returns the
+// fastest in var / len.  Every candidate writes the same derivatives bit for
+// bit, so the timing launches are the pass itself and leave the same
+// result.  Returns false (nothing to cache) when timing failed or the step
+// was inactive (its kernels returned at once, so the times mean nothing).
+template <int EMU>
+bool tune_axis(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along, int& var, int& len) {
+  const int64_t lines = (int64_t)lanes * other;
+  std::vector<std::array<int, 2>> cand;
+  for (int v = 0; v < 2; v++)
+    for (int64_t waves : {2, 4, 8, 16}) {
+      const std::array<int, 2> c{v, seg_len_for(lines, along, waves)};
+      bool seen = false;
+      for (const auto& d : cand) seen = seen || d == c;
+      if (!seen) cand.push_back(c);
+    }
+  const size_t n = cand.size();
+  std::vector<cudaEvent_t> ev(n + 1, nullptr);
+  bool ok = true;
+  for (auto& e : ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+  int active = 1;
+  if (ok) {
+    launch_axis<EMU>(s, ax, cand[0][0], a, lanes, other, along, cand[0][1]);
+    cudaEventRecord(ev[0], s);
+    for (size_t c = 0; c < n; c++) {
+      launch_axis<EMU>(s, ax, cand[c][0], a, lanes, other, along, cand[c][1]);
+      cudaEventRecord(ev[c + 1], s);
+    }
+    if (a.ctl) ok = cudaMemcpyAsync(&active, &a.ctl->active, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+    ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
+    float best = 0.0f;
+    for (size_t c = 0; ok && c < n; c++) {
+      float t = 0.0f;
+      ok = cudaEventElapsedTime(&t, ev[c], ev[c + 1]) == cudaSuccess;
+      if (ok && (c == 0 || t < best)) {
+        best = t;
+        var = cand[c][0];
+        len = cand[c][1];
+      }
+    }
+  }
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  return ok && active;
+}
+
 template <int EMU>
 void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[3], double* const dp[3],
              double* const dm[3], const Ctl* ctl) {
+  const int mode = axis_variant();
   for (int ax = 0; ax < 3; ax++) {
     const int along = ax == 0 ? b.fbx() : (ax == 1 ? b.fby() : b.fbz());
     const int lanes = ax == 0 ? b.fby() : b.fbx();
@@ -521,34 +608,31 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     // the shared-memory form is the faster one from ~12 M fill voxels on
     // (measured on GB300, register / shared-memory form, M voxel-steps/s:
     // 128^3 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
-    int var = axis_variant();
-    if (var < 0) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
-    // a segment recomputes 5 faces and 3 centres before its first voxel:
-    // segments as long as the line allows while the launch still fills about
-    // eight (register form) or four (shared-memory form) waves of 12 warps on
-    // every SM, and at least SEG voxels
-    int len = SEG;
-    if (EMU != 0) {
-      const int64_t lines = (int64_t)lanes * other;
-      const int64_t want = (var ? 4LL : 8LL) * 152 * 12 * 32;
-      int64_t nseg = (want + lines - 1) / lines;
-      const int64_t most = (along + SEG - 1) / SEG;
-      if (nseg > most) nseg = most;
-      if (nseg < 1) nseg = 1;
-      len = (int)((along + nseg - 1) / nseg);
-    }
+    int var = mode == 0 || mode == 1 ? mode : ((int64_t)lanes * other * along >= kRingVoxels ? 1 : 0);
+    int len = EMU == 0 ? SEG : seg_len_for((int64_t)lanes * other, along, var ? 4 : 8);
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
-    dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
-    cudaEvent_t e0 = ctl ? prof_open(s) : nullptr;
-    if (EMU == 0 || var == 0) {
-      if (ax == 0) k_weno_axis<0, EMU, false><<<g, 128, 0, s>>>(a);
-      else if (ax == 1) k_weno_axis<1, EMU, false><<<g, 128, 0, s>>>(a);
-      else k_weno_axis<2, EMU, false><<<g, 128, 0, s>>>(a);
-    } else {
-      if (ax == 0) k_weno_axis<0, EMU, EMU != 0><<<g, 128, 0, s>>>(a);
-      else if (ax == 1) k_weno_axis<1, EMU, EMU != 0><<<g, 128, 0, s>>>(a);
-      else k_weno_axis<2, EMU, EMU != 0><<<g, 128, 0, s>>>(a);
+    if (mode == 2 && EMU != 0) {
+      const TuneKey key{EMU, ax, lanes, other, along};
+      bool found = false;
+      {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        const auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+          var = it->second[0];
+          len = it->second[1];
+          found = true;
+        }
+      }
+      int tv = var, tl = len;
+      if (!found && tune_axis<EMU>(s, ax, a, lanes, other, along, tv, tl)) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune.emplace(key, std::array<int, 2>{tv, tl});
+        var = tv;
+        len = tl;
+      }
     }
+    cudaEvent_t e0 = ctl ? prof_open(s) : nullptr;
+    launch_axis<EMU>(s, ax, var, a, lanes, other, along, len);
     prof_close(s, e0, kProfAxisX + ax);
   }
 }
@@ -604,3 +688,27 @@ void launch_weno_combine(cudaStream_t s, int stage, bool final_stage, const Box&
 }
 
 }  // namespace qss
+
+extern "C" {
+
+int qssgpu_axis_tuning(int* rows, int max_rows) {
+  std::lock_guard<std::mutex> lk(qss::g_tune_mu);
+  int n = 0;
+  for (const auto& kv : qss::g_tune) {
+    if (rows && n < max_rows) {
+      int* r = rows + 7 * n;
+      for (int k = 0; k < 5; k++) r[k] = kv.first[k];
+      r[5] = kv.second[0];
+      r[6] = kv.second[1];
+    }
+    n++;
+  }
+  return n;
+}
+
+void qssgpu_axis_tuning_reset(void) {
+  std::lock_guard<std::mutex> lk(qss::g_tune_mu);
+  qss::g_tune.clear();
+}
+
+}  // extern "C"

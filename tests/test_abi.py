@@ -109,3 +109,19 @@ def test_host_side_argument_checks(lib):
                               full.ctypes.data_as(C.POINTER(C.c_ubyte)), None)
     assert rc != 0 and L.qssgpu_last_error() != 0
     L.qssgpu_clear_error()
+
+
+def test_axis_variant_settings(lib):
+    """The axis-pass form setting takes -1 (by size), 0, 1 and 2 (tuned),
+    clamps larger values to 2, returns the previous setting, and the tuned
+    shape table starts empty and can be cleared."""
+    L = Q.load(Q.GPU_LIB)
+    prev = L.qssgpu_set_axis_variant(2)
+    try:
+        assert L.qssgpu_set_axis_variant(7) == 2
+        assert L.qssgpu_set_axis_variant(0) == 2
+        assert L.qssgpu_set_axis_variant(-5) == 0
+    finally:
+        L.qssgpu_set_axis_variant(prev)
+    L.qssgpu_axis_tuning_reset()
+    assert L.qssgpu_axis_tuning(None, 0) == 0

@@ -110,7 +110,8 @@ def test_const_curv_model(gpu, oracle, theta, space, time):
     assert diff_arrays(vg, vo) == {}
 
 
-@pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 1), (1, 2, 0), (1, 2, 1)])
+@pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 1), (1, 2, 0), (1, 2, 1),
+                                               (1, 2, 2)])
 def test_const_curv_model_weno_modes(gpu, oracle, split, emu, variant):
     """WENO5 + TVD-RK3 with variable coefficients through the fused stage
     kernel and through the axis passes (both forms) + combine: all equal the
@@ -135,6 +136,44 @@ def test_const_curv_model_weno_modes(gpu, oracle, split, emu, variant):
     Q.check(gpu)
     assert tg == to
     assert diff_arrays(vg, vo) == {}
+
+
+def test_tuned_axis_shapes(gpu, oracle):
+    """Tuned axis passes: the first step times the candidate launch shapes of
+    each axis and keeps the fastest, later steps reuse it; the model still
+    equals the oracle, and the table holds each axis once with a valid form
+    and a segment length within the line."""
+    g, v = pack_case(oracle, 22, seed=6)
+    o_g = options(gpu, 40, 5, 3, tmax=0.02, tplot=0.01)
+    o_o = options(oracle, 40, 5, 3, tmax=0.02, tplot=0.01)
+    vg, vo = clone(v), clone(v)
+    prepare_model(oracle, o_g, vg, 1.25)
+    prepare_model(oracle, o_o, vo, 1.25)
+    gpu.setSpaceDerivFunc(C.byref(g), C.byref(o_g))
+    gpu.qssgpu_axis_tuning_reset()
+    prev = gpu.qssgpu_set_weno_split(1)
+    prev_emu = gpu.qssgpu_set_emu_level(2)
+    prev_var = gpu.qssgpu_set_axis_variant(2)
+    try:
+        tg = _model(gpu, vg, o_g, True, 1.25)
+    finally:
+        gpu.qssgpu_set_weno_split(prev)
+        gpu.qssgpu_set_emu_level(prev_emu)
+        gpu.qssgpu_set_axis_variant(prev_var)
+    to = _model(oracle, vo, o_o, True, 1.25)
+    Q.check(gpu)
+    assert tg == to
+    assert diff_arrays(vg, vo) == {}
+    n = gpu.qssgpu_axis_tuning(None, 0)
+    rows = (C.c_int * (7 * max(n, 1)))()
+    assert gpu.qssgpu_axis_tuning(rows, n) == n
+    r = np.array(rows[:7 * n]).reshape(n, 7)
+    assert sorted(r[:, 1].tolist()) == [0, 1, 2]
+    assert set(r[:, 0].tolist()) == {2}
+    assert set(r[:, 5].tolist()) <= {0, 1}
+    assert ((r[:, 6] >= 1) & (r[:, 6] <= r[:, 4])).all()
+    gpu.qssgpu_axis_tuning_reset()
+    assert gpu.qssgpu_axis_tuning(None, 0) == 0
 
 
 @pytest.mark.parametrize("slabs", [2, 5])
