@@ -195,6 +195,8 @@ def gpu_arm(args, dist: Dist):
     lib = Q.load(Q.GPU_LIB)
     if not lib.qssgpu_device_available():
         raise RuntimeError("GB300 library: no CUDA device")
+    if args.axis_variant is not None:
+        lib.qssgpu_set_axis_variant(args.axis_variant)
     n = args.n
     mask, phi = make_workload(n)
     g = Q.make_grid(lib, n)
@@ -275,8 +277,15 @@ def gpu_arm(args, dist: Dist):
                 "peak_source": peak_src,
                 "hbm": {"achieved": round(achieved_gbs, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                         "frac": round(achieved_gbs / peaks["hbm_gbs"], 4), "peak_kind": kind}}
+    tuned = []
+    nt = lib.qssgpu_axis_tuning(None, 0)
+    if nt:
+        rows = (C.c_int * (7 * nt))()
+        nt = min(nt, lib.qssgpu_axis_tuning(rows, nt))
+        tuned = [dict(zip(("level", "axis", "lanes", "lines_per_lane", "line", "form", "seg_len"),
+                          rows[7 * i:7 * i + 7])) for i in range(nt)]
     return {"value": value, "ms": ms, "e2e": e2e, "roofline": roofline, "clocks": clk.summary(),
-            "gpu_launches": launches, "stage_ms": top_ms}
+            "gpu_launches": launches, "stage_ms": top_ms, "axis_tuning": tuned}
 
 
 # host arrays the e2e call uploads (drain_model3d's coefficients and masks)
@@ -633,6 +642,9 @@ def main():
     ap.add_argument("--adj-n", type=int, default=128)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-ckpt", type=int, default=20)
+    ap.add_argument("--axis-variant", type=int, default=None,
+                    help="WENO5 axis passes: 0 registers, 1 shared memory, 2 launch shapes tuned by timing "
+                         "(default: form by size)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the roofline kernel (overrides the measured table)")
     args = ap.parse_args()
@@ -683,9 +695,13 @@ def main():
                 "config": {"workload": f"{args.n}^3 lognormal grain pack (mu=ln 8, sigma=0.3 voxels), porosity 0.30, "
                                        "theta 40 deg, WENO5 + TVD-RK3, variable coefficients",
                            "n": args.n, "ghost": 3, "dx": 0.04, "parallelism": f"replicas x{dist.ws}",
-                           "l2": "inputs larger than L2 (each FP64 array 1.1 GB)"},
+                           "l2": "inputs larger than L2 (each FP64 array 1.1 GB)",
+                           "axis_variant": {None: "by size", 0: "registers", 1: "shared memory",
+                                            2: "tuned"}.get(args.axis_variant, args.axis_variant)},
                 "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "roofline": res["roofline"],
                 "cpu_baseline": cpu, "clocks": res["clocks"]}
+        if res["axis_tuning"]:
+            line["config"]["axis_tuning"] = res["axis_tuning"]
         if args.batched:
             line["batched_mode"] = batched_arm(args)
         if args.adjoint:

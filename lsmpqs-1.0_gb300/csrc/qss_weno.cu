@@ -518,14 +518,24 @@ constexpr int64_t kRingVoxels = 12LL << 20;
 
 // a segment recomputes 5 faces and 3 centres before its first voxel:
 // segments as long as the line allows while the launch still fills about
-// `waves` waves of 12 warps on every SM, and at least SEG voxels
-int seg_len_for(int64_t lines, int along, int64_t waves) {
+// `waves` waves of 12 warps on every SM, and at most `most` segments a line
+int seg_len_for(int64_t lines, int along, int64_t waves, int64_t most) {
   const int64_t want = waves * 152 * 12 * 32;
   int64_t nseg = (want + lines - 1) / lines;
-  const int64_t most = (along + SEG - 1) / SEG;
   if (nseg > most) nseg = most;
   if (nseg < 1) nseg = 1;
   return (int)((along + nseg - 1) / nseg);
+}
+
+// The default segment length of each form follows the tuned mode's picks on
+// cubes (GB300).  Register form: ~8 waves, segments of about SEG voxels or
+// more (192^3: the tuned pick is this rule's).  Shared-memory form: ~16
+// waves with segments of at least 64 voxels; tuned picks 64 / 55 / 128
+// voxels at 256^3 / 384^3 / 512^3 (this rule: 64 / 64 / 128), where the
+// earlier rule of ~4 waves gave 64 / 192 / 512 and the stage ran at
+// 473 / 456 / 487 M voxel-steps/s against 473 / 487 / 496 tuned.
+int default_seg_len(int var, int64_t lines, int along) {
+  return var ? seg_len_for(lines, along, 16, along / 64) : seg_len_for(lines, along, 8, (along + SEG - 1) / SEG);
 }
 
 template <int EMU>
@@ -560,13 +570,16 @@ template <int EMU>
 bool tune_axis(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along, int& var, int& len) {
   const int64_t lines = (int64_t)lanes * other;
   std::vector<std::array<int, 2>> cand;
-  for (int v = 0; v < 2; v++)
-    for (int64_t waves : {2, 4, 8, 16}) {
-      const std::array<int, 2> c{v, seg_len_for(lines, along, waves)};
-      bool seen = false;
-      for (const auto& d : cand) seen = seen || d == c;
-      if (!seen) cand.push_back(c);
-    }
+  auto add = [&](int v, int l) {
+    const std::array<int, 2> c{v, l};
+    bool seen = false;
+    for (const auto& d : cand) seen = seen || d == c;
+    if (!seen) cand.push_back(c);
+  };
+  for (int v = 0; v < 2; v++) {
+    add(v, default_seg_len(v, lines, along));
+    for (int64_t waves : {2, 4, 8, 16, 32}) add(v, seg_len_for(lines, along, waves, (along + SEG - 1) / SEG));
+  }
   const size_t n = cand.size();
   std::vector<cudaEvent_t> ev(n + 1, nullptr);
   bool ok = true;
@@ -609,7 +622,7 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     // (measured on GB300, register / shared-memory form, M voxel-steps/s:
     // 128^3 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
     int var = mode == 0 || mode == 1 ? mode : ((int64_t)lanes * other * along >= kRingVoxels ? 1 : 0);
-    int len = EMU == 0 ? SEG : seg_len_for((int64_t)lanes * other, along, var ? 4 : 8);
+    int len = EMU == 0 ? SEG : default_seg_len(var, (int64_t)lanes * other, along);
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
     if (mode == 2 && EMU != 0) {
       const TuneKey key{EMU, ax, lanes, other, along};
