@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <initializer_list>
+#include <string>
 
 #include "../../include/lsmpqs_gpu.h"
 #include "../../include/lsmpqs_types.h"
@@ -77,6 +78,20 @@ void flatten_2d(Grid* g) {
   }
 }
 
+// `prog 'name'`: the name in single quotes (each ' as '\''), so that names
+// with spaces or shell metacharacters reach the program as one argument
+void run_on_file(const char* prog, const char* name) {
+  std::string cmd = prog;
+  cmd += " '";
+  for (const char* c = name; *c; c++) {
+    if (*c == '\'') cmd += "'\\''";
+    else cmd += *c;
+  }
+  cmd += "'";
+  if (system(cmd.c_str())) {
+  }
+}
+
 int valid_dims(int d) {
   if (d == 2 || d == 3) return d;
   fprintf(stderr, "\nInvalid number of dimensions (%d).  Using to default value of 2.\n", d);
@@ -88,40 +103,33 @@ int valid_dims(int d) {
 extern "C" {
 
 // ---------------------------------------------------------------- files
+// As the reference: a name containing ".gz" (else ".bz2") is decompressed in
+// place by the program and the base name is the name less its last 3 (4)
+// characters.  The base is allocated to fit (the reference's fixed 256 bytes
+// overflow on longer paths); free() it.
 void checkUnzipFile(char* file_name, int* pzip_status, char** pfile_base) {
-  char cmd[600];
-  char* base = (char*)malloc(256);
+  const size_t len = strlen(file_name);
+  char* base = (char*)malloc(len + 1);
   int zs = NO_ZIP;
+  size_t keep = len;
   if (strstr(file_name, ".gz")) {
     zs = GZIP;
-    snprintf(cmd, sizeof cmd, "gunzip -f %s", file_name);
-    if (system(cmd)) {
-    }
-    size_t L = strlen(file_name) - 3;
-    memcpy(base, file_name, L);
-    base[L] = 0;
+    run_on_file("gunzip -f", file_name);
+    keep = len - 3;
   } else if (strstr(file_name, ".bz2")) {
     zs = BZIP2;
-    snprintf(cmd, sizeof cmd, "bunzip2 -f %s", file_name);
-    if (system(cmd)) {
-    }
-    size_t L = strlen(file_name) - 4;
-    memcpy(base, file_name, L);
-    base[L] = 0;
-  } else {
-    snprintf(base, 256, "%s", file_name);
+    run_on_file("bunzip2 -f", file_name);
+    keep = len - 4;
   }
+  memcpy(base, file_name, keep);
+  base[keep] = 0;
   *pzip_status = zs;
   *pfile_base = base;
 }
 
 void zipFile(char* file_base, int zip_status) {
-  char cmd[600];
-  if (zip_status == GZIP) snprintf(cmd, sizeof cmd, "gzip -f %s", file_base);
-  else if (zip_status == BZIP2) snprintf(cmd, sizeof cmd, "bzip2 -f %s", file_base);
-  else return;
-  if (system(cmd)) {
-  }
+  if (zip_status == GZIP) run_on_file("gzip -f", file_base);
+  else if (zip_status == BZIP2) run_on_file("bzip2 -f", file_base);
 }
 
 // ---------------------------------------------------------------- grid
@@ -387,11 +395,17 @@ static void* read_array(int* dims, char* file_name, size_t elem) {
   checkUnzipFile(file_name, &zs, &base);
   FILE* fp = fopen(base, "r");
   if (fp) {
-    if (fread(dims, sizeof(int), 3, fp) != 3) {
-    }
-    const size_t n = (size_t)dims[0] * dims[1] * dims[2];
-    data = malloc(n * elem);
-    if (fread(data, elem, n, fp) != n) {
+    // a header that is missing or not three positive sizes reads as no array
+    // (NULL) instead of sizing an allocation from it; a short payload leaves
+    // the rest zero
+    if (fread(dims, sizeof(int), 3, fp) == 3 && dims[0] > 0 && dims[1] > 0 && dims[2] > 0) {
+      const size_t n = (size_t)dims[0] * dims[1] * dims[2];
+      data = calloc(n, elem);
+      if (data && fread(data, elem, n, fp) != n) {
+        printf("\nFile %s is shorter than its header says", file_name);
+      }
+    } else {
+      printf("\nFile %s has no valid array header", file_name);
     }
     fclose(fp);
     zipFile(base, zs);
@@ -478,7 +492,11 @@ Options* createOptionsFromInputFile(char* filename) {
     return o;
   }
   char line[100], word[100];
-  while (fgets(line, 80, fp)) {
+  // keywords are told apart by letters at fixed positions; past the end of
+  // a short line those read as 0, never as a previous line's letters
+  for (;;) {
+    memset(line, 0, sizeof line);
+    if (!fgets(line, 80, fp)) break;
     int n = 0;
     while (isspace((unsigned char)line[n])) n++;
     const char* s = line + n;

@@ -2,6 +2,7 @@
 import os
 import subprocess
 import sys
+import tempfile
 
 import pytest
 
@@ -14,10 +15,17 @@ for p in (PKG, os.path.join(ROOT, "tests")):
 
 ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libqss_ref.so")
+SCRATCH = os.path.join(ROOT, ".test_tmp")
 
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the GB300 kernels)")
+    # the tests' scratch files (per-step files, array files, option decks)
+    # stay inside the repository: tempfile's directories and pytest's tmp_path
+    os.makedirs(SCRATCH, exist_ok=True)
+    tempfile.tempdir = SCRATCH
+    if not config.option.basetemp:
+        config.option.basetemp = os.path.join(SCRATCH, "pytest")
 
 
 def _ensure_oracle():

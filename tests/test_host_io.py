@@ -174,3 +174,79 @@ def test_gzip_members_round_trip(host, tmp_path):
         assert np.array_equal(np.ctypeslib.as_array(back, (n,)), data)
     finally:
         os.chdir(cwd)
+
+
+def _reader(host):
+    rd = host.readDataArrayQSS
+    rd.restype = Q.c_double_p
+    rd.argtypes = [C.POINTER(C.c_int), C.c_char_p]
+    return rd
+
+
+def _small_grid(host):
+    dims = (C.c_int * 3)(6, 5, 4)
+    lo = (C.c_double * 3)(0.0, 0.0, 0.0)
+    hi = (C.c_double * 3)(0.24, 0.20, 0.16)
+    return host.createGridSetGridDims(3, dims, lo, hi, 1)
+
+
+def test_file_names_passed_to_gzip_as_one_argument(host, tmp_path):
+    """Compressed array files whose names hold a space, a single quote or a
+    shell metacharacter, or whose path is longer than 256 bytes, are
+    decompressed, read and compressed again in place by the gzip programs,
+    the name reaching them as one argument."""
+    gh = _small_grid(host)
+    n = gh[0].num_gridpts
+    data = np.random.default_rng(9).standard_normal(n)
+    deep = tmp_path / ("d" * 120) / ("e" * 120)
+    deep.mkdir(parents=True)
+    host.writeDataArrayQSS.argtypes = [Q.c_double_p, C.POINTER(Q.Grid), C.c_char_p, C.c_int]
+    rd = _reader(host)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        for path in ("a b", "it's", "x;touch pwned", str(deep / "long")):
+            assert len(str(deep / "long")) > 256
+            host.writeDataArrayQSS(Q.dptr(data), gh, path.encode(), 1)
+            assert os.path.exists(path + ".gz") and not os.path.exists(path)
+            d3 = (C.c_int * 3)()
+            back = rd(d3, (path + ".gz").encode())
+            assert back, path
+            assert list(d3) == list(gh[0].grid_dims_ghostbox)
+            assert np.array_equal(np.ctypeslib.as_array(back, (n,)), data), path
+            assert os.path.exists(path + ".gz") and not os.path.exists(path), path
+        assert not os.path.exists("pwned")
+    finally:
+        os.chdir(cwd)
+
+
+def test_bad_array_headers_read_as_null(host, tmp_path):
+    """An array file without a valid header (too short, or a size that is not
+    positive) reads as NULL instead of sizing an allocation from it; a
+    payload shorter than the header says leaves the rest zero."""
+    rd = _reader(host)
+    p = tmp_path / "bad"
+    for content in (b"", b"\x01\x00\x00\x00", np.array([4, -1, 2], np.int32).tobytes(),
+                    np.array([0, 5, 5], np.int32).tobytes()):
+        p.write_bytes(content)
+        d3 = (C.c_int * 3)()
+        assert not rd(d3, str(p).encode())
+    p.write_bytes(np.array([2, 2, 2], np.int32).tobytes() + np.arange(3, dtype=np.float64).tobytes())
+    d3 = (C.c_int * 3)()
+    back = rd(d3, str(p).encode())
+    assert list(d3) == [2, 2, 2]
+    assert np.ctypeslib.as_array(back, (8,)).tolist() == [0.0, 1.0, 2.0] + [0.0] * 5
+
+
+def test_option_file_short_lines(host, tmp_path):
+    """Lines shorter than the letter positions that tell keywords apart
+    ('c', 'd', 'do 0', 'v 1', 'u 1', 'e 1') set nothing, whatever the lines
+    before them held."""
+    p = tmp_path / "deck"
+    p.write_text("err_check_zone 0.7\nc\nvol_frac_max 0.8\nd\ndo 0\nuse_var_theta 1\nv 1\nu 1\ne 1\na 0.3\n")
+    o = _parse(host, str(p))
+    d = _parse(host, str(tmp_path / "missing"))  # the defaults
+    assert o.a == 0.3 and o.err_check_zone == 0.7 and o.vol_frac_max == 0.8 and o.use_var_theta == 1
+    for f in FIELDS:
+        if f not in ("a", "err_check_zone", "vol_frac_max", "use_var_theta"):
+            assert getattr(o, f) == getattr(d, f), f
