@@ -171,7 +171,7 @@ static void dalloc(T*& ptr, int64_t count) {
 }
 
 static void destroy_volume(DevVolume* v) {
-  cudaStreamSynchronize(v->stream);
+  if (v->stream) cudaStreamSynchronize(v->stream);
   void* ptrs[] = {v->phi, v->s1, v->s2, v->phi_prev, v->mask, v->mask_w, v->mask_nw, v->mask_disconn,
                   v->mask_x, v->mask_y, v->mask_z, v->phi_extra, v->vel_n, v->bcoef, v->vx, v->vy,
                   v->vz, v->scratch, v->r_phi0, v->r_dist, v->r_next, v->contrib, v->labels, v->nsrc,
@@ -184,9 +184,11 @@ static void destroy_volume(DevVolume* v) {
   }
   if (v->h_ctl) cudaFreeHost(v->h_ctl);
   if (v->h_scal) cudaFreeHost(v->h_scal);
-  cudaStreamDestroy(v->stream);
+  if (v->stream) cudaStreamDestroy(v->stream);
   delete v;
 }
+
+static void alloc_volume(DevVolume* v);
 
 static bool same_box(const Box& a, const Box& b) {
   return a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.ilo == b.ilo && a.ihi == b.ihi &&
@@ -209,6 +211,22 @@ DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g) {
   v->box = b;
   v->n = b.npts();
   v->nfb = (int64_t)b.fbx() * b.fby() * b.fbz();
+  try {
+    alloc_volume(v);
+  } catch (...) {
+    // an allocation that failed (device memory exhausted) frees what was
+    // already taken and clears the runtime's last error, so that later calls
+    // (on smaller volumes, or after a release) start clean
+    destroy_volume(v);
+    cudaGetLastError();
+    throw;
+  }
+  g_table[p] = v;
+  return *v;
+}
+
+static void alloc_volume(DevVolume* v) {
+  const Box& b = v->box;
   const int64_t n = v->n;
   QSS_CK(cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking));
   double** reals[] = {&v->phi, &v->s1, &v->s2, &v->phi_prev, &v->mask, &v->mask_w, &v->mask_nw,
@@ -236,8 +254,6 @@ DevVolume& volume_for(const QSS_DataArrays* p, const Grid* g) {
   QSS_CK(cudaMemsetAsync(v->s1, 0, n * sizeof(double), v->stream));
   QSS_CK(cudaMemsetAsync(v->s2, 0, n * sizeof(double), v->stream));
   QSS_CK(cudaStreamSynchronize(v->stream));
-  g_table[p] = v;
-  return *v;
 }
 
 void release_volume(const QSS_DataArrays* p) {
