@@ -246,6 +246,12 @@ int qssgpu_ladder_batch(int drain, int n, Options* const* o, QSS_DataArrays* con
     return n > 0 ? n : 1;
   }
   for (int i = 0; i < n; i++)
+    if (!o[i] || !p[i] || !g[i]) {
+      set_error(QSSGPU_ERR_ARG, "qssgpu_ladder_batch: volume " + std::to_string(i) + " has a NULL option, array "
+                                "or grid pointer");
+      return n;
+    }
+  for (int i = 0; i < n; i++)
     for (int j = 0; j < i; j++)
       if (p[i] == p[j] || o[i] == o[j]) {
         set_error(QSSGPU_ERR_ARG, "qssgpu_ladder_batch: volumes must not share arrays or options");
@@ -266,6 +272,9 @@ int qssgpu_ladder_batch(int drain, int n, Options* const* o, QSS_DataArrays* con
       volume_for(p[v], g[v]);
     } catch (const Error& e) {
       codes[v] = e.code ? e.code : 1;
+      msgs[v] = e.what();
+    } catch (const std::exception& e) {  // host memory for the volume's state
+      codes[v] = QSSGPU_ERR_CUDA;
       msgs[v] = e.what();
     }
     setup[v] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -86,7 +86,7 @@ def test_no_device_is_reported_not_crashed(lib):
 
 def test_host_side_argument_checks(lib):
     """Checks that run before any device work: the batch rejects volumes that
-    share arrays or options, and without a GPU the page-locked allocator and
+    share arrays or options or have a NULL pointer, and without a GPU the page-locked allocator and
     the phase-image call fail cleanly with an error code."""
     L = Q.load(Q.GPU_LIB)
     g = Q.make_grid(L, 8)
@@ -98,6 +98,12 @@ def test_host_side_argument_checks(lib):
     L.qssgpu_clear_error()
     assert L.qssgpu_ladder_batch(1, 2, arr_o, arr_p, arr_g, None, None, 0) == 2
     assert b"share" in L.qssgpu_error_string()
+    L.qssgpu_clear_error()
+    w = Q.Volume(g)
+    arr_p = (C.POINTER(Q.QSSDataArrays) * 2)(C.pointer(v.p), C.pointer(w.p))
+    arr_g = (C.POINTER(Q.Grid) * 2)(C.pointer(g), None)  # a NULL grid entry
+    assert L.qssgpu_ladder_batch(1, 2, arr_o, arr_p, arr_g, None, None, 0) == 2
+    assert b"NULL" in L.qssgpu_error_string()
     L.qssgpu_clear_error()
     if L.qssgpu_device_available():
         return
