@@ -1000,9 +1000,8 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
     cudaStreamDestroy(a.s);
     if (host_err) throw Error(QSSGPU_ERR_DEVICE_CHECK, "device check failed in the adjoint run");
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 

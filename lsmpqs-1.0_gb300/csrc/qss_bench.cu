@@ -62,8 +62,8 @@ int qssgpu_fp64_peak(double* out) {
     cudaEventDestroy(e1);
     cudaFree(d);
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
+  } catch (const std::exception& e) {
+    report_exception(e);
     return 1;
   }
 }

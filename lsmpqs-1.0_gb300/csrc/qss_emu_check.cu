@@ -180,8 +180,8 @@ int qssgpu_emu_selftest(long long n, unsigned long long seed, long long* counts,
     if (first)
       for (int q = 0; q < 3; q++) first[q] = hf[q];
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
+  } catch (const std::exception& e) {
+    report_exception(e);
     return 1;
   }
 }
@@ -204,8 +204,8 @@ int qssgpu_op_rates(double* out) {
     for (int q = 0; q < 7; q++) out[q] = ops / (t[q] * 1e-3) / 1e9;
     cudaFree(d);
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
+  } catch (const std::exception& e) {
+    report_exception(e);
     return 1;
   }
 }

@@ -94,9 +94,8 @@ int qssgpu_volume_noalloc(const double* d_phi, const int gb[6], const int ib[6],
     launch_volume(s, b, d_phi, dx, dy, dz, epsilon, scratch, d_volume);
     QSS_CK(cudaGetLastError());
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 

@@ -187,8 +187,8 @@ void qss_reinitialize_mask(QSS_DataArrays* p, Grid* g, Options* o) {
     d2h(st.s, p->lse_rhs, rhs, bytes);
     d2h(st.s, p->phi_next, next, bytes);
     QSS_CK(cudaStreamSynchronize(st.s));
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
+  } catch (const std::exception& e) {
+    report_exception(e);
   }
 }
 
@@ -221,9 +221,8 @@ int qssgpu_create_mask_ubc(const unsigned char* ubc, QSS_DataArrays* p, Grid* g,
     d2h(st.s, p->phi_next, next, bytes);
     QSS_CK(cudaStreamSynchronize(st.s));
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 
@@ -258,9 +257,8 @@ int qssgpu_create_init_from_mask(QSS_DataArrays* p, Grid* g, Options* o) {
     d2h(st.s, p->phi, phi, bytes);
     QSS_CK(cudaStreamSynchronize(st.s));
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 
@@ -306,9 +304,8 @@ int qssgpu_diff_steps(const double* step_a, const double* step_b, Grid* g, doubl
       QSS_CK(cudaStreamSynchronize(st.s));
     }
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 
@@ -338,9 +335,8 @@ int qssgpu_phase_uchar(const double* phi, const double* mask, Grid* g, char phas
     if (dfb) d2h(st.s, bin_fb, dfb, (size_t)nfb);
     QSS_CK(cudaStreamSynchronize(st.s));
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 

@@ -33,6 +33,16 @@ enum {
 void set_error(int code, const std::string& msg);
 void clear_error();
 
+// Records an exception escaping an entry point as the calling thread's error
+// (the library's Error with its code; any other, such as host memory
+// exhausted, as QSSGPU_ERR_CUDA) and returns the code.
+inline int report_exception(const std::exception& e) {
+  const Error* q = dynamic_cast<const Error*>(&e);
+  const int code = q && q->code ? q->code : QSSGPU_ERR_CUDA;
+  set_error(code, e.what());
+  return code;
+}
+
 #define QSS_CK(expr)                                                                            \
   do {                                                                                          \
     cudaError_t e_ = (expr);                                                                    \

@@ -279,9 +279,8 @@ int qssgpu_loop_sum(const double* values, long long n, double* out) {
     cudaFree(dout);
     cudaStreamDestroy(s);
     return 0;
-  } catch (const Error& e) {
-    set_error(e.code, e.what());
-    return e.code ? e.code : 1;
+  } catch (const std::exception& e) {
+    return report_exception(e);
   }
 }
 
