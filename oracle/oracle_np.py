@@ -79,24 +79,87 @@ def weno5_plus_minus(phi, fb, d, inv):
     return plus, minus
 
 
+def eno2_plus_minus(phi, fb, d, inv):
+    """ENO2 phi_plus and phi_minus along axis d (3d.f:1113-1182, the same
+    text in the constant-coefficient variant 3d.f:394-463): second
+    differences taken from phi directly, the smaller one in magnitude
+    chosen (ties take the second)."""
+    def s(m):
+        return _shift(phi, fb, *_axis(d, m))
+
+    D1 = s(0) - s(-1)
+    D1p = s(1) - s(0)
+    D2 = (s(1) + s(-1)) - 2.0 * s(0)
+    D2p = (s(2) + s(0)) - 2.0 * s(1)
+    D2m = (s(-2) + s(0)) - 2.0 * s(-1)
+    plus = np.where(np.abs(D2) < np.abs(D2p), (D1p - 0.5 * D2) * inv, (D1p - 0.5 * D2p) * inv)
+    minus = np.where(np.abs(D2m) < np.abs(D2), (D1 + 0.5 * D2m) * inv, (D1 + 0.5 * D2) * inv)
+    return plus, minus
+
+
+def eno3_plus_minus(phi, fb, d, inv, inv_minus):
+    """ENO3 phi_plus and phi_minus along axis d (3d.f:1446-1700, the same
+    text in the constant-coefficient variant 3d.f:676-931).  Kept as the
+    Fortran has them: the x stencil's outermost plus point is phi(i+3,j,j)
+    (3d.f:1454), and the y and z minus derivatives are scaled by 1/dx
+    (inv_minus = 1/dx for every axis)."""
+    def s(m):
+        return _shift(phi, fb, *_axis(d, m))
+
+    if d == 0:
+        ilo, ihi, jlo, jhi, klo, khi = fb
+        J = np.arange(jlo, jhi + 1)[:, None]
+        I = np.arange(ilo, ihi + 1)[None, :]
+        far = np.broadcast_to(phi[J, J, I + 3][None, :, :], s(0).shape)
+    else:
+        far = s(3)
+    D1 = s(0) - s(-1)
+    D1p = s(1) - s(0)
+    D1m = s(-1) - s(-2)
+    D1mm = s(-2) - s(-3)
+    D1pp = s(2) - s(1)
+    D1ppp = far - s(2)
+    D2 = D1p - D1
+    D2p = D1pp - D1p
+    D2m = D1 - D1m
+    D2pp = D1ppp - D1pp
+    D2mm = D1m - D1mm
+    D3 = D2 - D2m
+    D3p = D2p - D2
+    D3pp = D2pp - D2p
+    D3m = D2m - D2mm
+    third, sixth = 1.0 / 3.0, 1.0 / 6.0
+
+    a = D1p - 0.5 * D2
+    a = np.where(np.abs(D3) < np.abs(D3p), a - sixth * D3, a - sixth * D3p)
+    c = D1p - 0.5 * D2p
+    c = np.where(np.abs(D3p) < np.abs(D3pp), c + third * D3p, c + third * D3pp)
+    plus = np.where(np.abs(D2) < np.abs(D2p), a, c) * inv
+
+    a = D1 + 0.5 * D2m
+    a = np.where(np.abs(D3m) < np.abs(D3), a + third * D3m, a + third * D3)
+    c = D1 + 0.5 * D2
+    c = np.where(np.abs(D3) < np.abs(D3p), c - sixth * D3, c - sixth * D3p)
+    minus = np.where(np.abs(D2m) < np.abs(D2), a, c) * inv_minus
+    return plus, minus
+
+
 def _sq(x):
     return x * x
 
 
-def rhs_weno5(phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
-    """getRHS3d5th (3d.f:1827-2385) on the fill box: returns (lse_rhs over the
-    fill box, max_H_over_dX).
-
-    Kept as the Fortran has them: +vel_n*|grad phi| (3d.f:2276); temp_norm
-    keeps the previous voxel's value (loop order) where |vel_n| < 1e-5, 0
-    before the first voxel that sets it; max_H_over_dX is reset inside the
-    loop, so the last voxel's H is returned."""
+def _assemble(pm, phi, vn, b, adv, fb, dx, dy, dz, norm_sign):
+    """The part every right-hand-side variant shares (3d.f:2249-2385 for
+    WENO5; the same text for ENO2 3d.f:1183-1320 and ENO3 3d.f:1701-1812,
+    and without the advection term for the constant-coefficient variants):
+    Godunov normal term (sign +1 for WENO5, -1 otherwise), CFL estimate of
+    the last voxel, upwind advection (adv = (vx, vy, vz) or None), central
+    curvature.  vn and b are arrays over the fill box."""
     inv = (1.0 / dx, 1.0 / dy, 1.0 / dz)
     fac = (0.5 / dx, 0.5 / dy, 0.5 / dz)
-    (pxp, pxm), (pyp, pym), (pzp, pzm) = (weno5_plus_minus(phi, fb, d, inv[d]) for d in range(3))
-    vn = _shift(vel_n, fb)
+    (pxp, pxm), (pyp, pym), (pzp, pzm) = pm
 
-    # Godunov |grad phi|^2 (3d.f:2253-2270)
+    # Godunov |grad phi|^2
     zero = 0.0
     pos = ((np.maximum(_sq(np.maximum(pxm, zero)), _sq(np.minimum(pxp, zero)))
             + np.maximum(_sq(np.maximum(pym, zero)), _sq(np.minimum(pyp, zero))))
@@ -106,13 +169,14 @@ def rhs_weno5(phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
            + np.maximum(_sq(np.minimum(pzm, zero)), _sq(np.maximum(pzp, zero))))
     ngps = np.where(vn > 0.0, pos, neg)
     set_here = np.abs(vn) >= ZERO_TOL
-    norm_here = (vn * np.sqrt(ngps)).ravel()
+    signed_vn = vn if norm_sign > 0 else -vn
+    norm_here = (signed_vn * np.sqrt(ngps)).ravel()
     # carried temp_norm in loop order (i fastest, then j, then k)
     flat_set = set_here.ravel()
     last = np.maximum.accumulate(np.where(flat_set, np.arange(flat_set.size), -1))
     temp_norm = np.where(last >= 0, norm_here[np.maximum(last, 0)], 0.0).reshape(vn.shape)
 
-    # CFL estimate of the last voxel (3d.f:2280-2304)
+    # CFL estimate of the last voxel
     mdx = max(dx, dy, dz)
     max_dx_sq = mdx * mdx
     cx = np.maximum(np.abs(pxp), np.abs(pxm))[-1, -1, -1]
@@ -122,14 +186,7 @@ def rhs_weno5(phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
     h = abs(vn[-1, -1, -1]) / ngp * ((cx * inv[0] + cy * inv[1]) + cz * inv[2])
     max_h = h if h > -1.0 else -1.0
 
-    # upwind advection (3d.f:2308-2332)
-    ux, uy, uz = _shift(vx, fb), _shift(vy, fb), _shift(vz, fb)
-    pxa = np.where(ux >= 0, pxm, pxp)
-    pya = np.where(uy >= 0, pym, pyp)
-    pza = np.where(uz >= 0, pzm, pzp)
-    temp_vel = -((ux * pxa + uy * pya) + uz * pza)
-
-    # central curvature (3d.f:2336-2374)
+    # central curvature
     def s(di=0, dj=0, dk=0):
         return _shift(phi, fb, di, dj, dk)
 
@@ -155,8 +212,55 @@ def rhs_weno5(phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
     curv = curv - ((2.0 * pyz) * py) * pz
     with np.errstate(divide="ignore", invalid="ignore"):
         curv = np.where(g2 < ZERO_TOL, 0.0, curv / g2)
-    temp_curv = _shift(b, fb) * curv
+    temp_curv = b * curv
+    if adv is None:
+        return temp_norm + temp_curv, max_h
+
+    # upwind advection
+    ux, uy, uz = adv
+    pxa = np.where(ux >= 0, pxm, pxp)
+    pya = np.where(uy >= 0, pym, pyp)
+    pza = np.where(uz >= 0, pzm, pzp)
+    temp_vel = -((ux * pxa + uy * pya) + uz * pza)
     return (temp_norm + temp_curv) + temp_vel, max_h
+
+
+def _derivs(scheme, phi, fb, dx, dy, dz):
+    inv = (1.0 / dx, 1.0 / dy, 1.0 / dz)
+    if scheme == 2:
+        return [eno2_plus_minus(phi, fb, d, inv[d]) for d in range(3)]
+    if scheme == 3:
+        return [eno3_plus_minus(phi, fb, d, inv[d], inv[0]) for d in range(3)]
+    return [weno5_plus_minus(phi, fb, d, inv[d]) for d in range(3)]
+
+
+def rhs_var(scheme, phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
+    """getRHS3d2nd / getRHS3d3rd / getRHS3d5th (scheme 2, 3, 5; 3d.f:1020,
+    1335, 1827) on the fill box: returns (lse_rhs over the fill box,
+    max_H_over_dX).
+
+    Kept as the Fortran has them: the normal term is -vel_n*|grad phi|
+    except +vel_n*|grad phi| in getRHS3d5th (3d.f:2276); temp_norm keeps the
+    previous voxel's value (loop order) where |vel_n| < 1e-5, 0 before the
+    first voxel that sets it; max_H_over_dX is reset inside the loop, so the
+    last voxel's H is returned."""
+    pm = _derivs(scheme, phi, fb, dx, dy, dz)
+    adv = (_shift(vx, fb), _shift(vy, fb), _shift(vz, fb))
+    return _assemble(pm, phi, _shift(vel_n, fb), _shift(b, fb), adv, fb, dx, dy, dz, 1 if scheme == 5 else -1)
+
+
+def rhs_weno5(phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
+    """getRHS3d5th (3d.f:1827-2385), see rhs_var."""
+    return rhs_var(5, phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz)
+
+
+def rhs_const(scheme, phi, a, bconst, fb, dx, dy, dz):
+    """getRHS3d2ndConst / getRHS3d3rdConst (scheme 2, 3; 3d.f:302, 572):
+    constant normal speed a and curvature coefficient b, no advection;
+    returns (lse_rhs over the fill box, max_H_over_dX)."""
+    pm = _derivs(scheme, phi, fb, dx, dy, dz)
+    shape = _shift(phi, fb).shape
+    return _assemble(pm, phi, np.full(shape, float(a)), np.full(shape, float(bconst)), None, fb, dx, dy, dz, -1)
 
 
 def rk1(u_cur, rhs, dt):

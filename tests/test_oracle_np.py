@@ -1,8 +1,9 @@
 """The C restatement of the Fortran kernels (oracle_kernels3d.c) against a
 second, independent restatement in numpy (oracle/oracle_np.py), bit for bit
-on random inputs: the WENO5 right-hand side of the variable-coefficient
-model (with voxels below the speed tolerance, zero and negative advection
-speeds, unequal spacings, z-slabs), the TVD-RK stages and the signed linear
+on random inputs: the ENO2, ENO3 and WENO5 right-hand sides of the
+variable-coefficient model (with voxels below the speed tolerance, zero and
+negative advection speeds, unequal spacings, z-slabs) and the ENO2/ENO3
+constant-coefficient ones, the TVD-RK stages and the signed linear
 extrapolation of every face.  No GPU."""
 import ctypes as C
 import os
@@ -16,7 +17,8 @@ import qssgpu as Q
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
 import oracle_np as N  # noqa: E402
 
-SHAPES = [(14, 11, 9), (7, 16, 12)]
+# (the ENO3 x stencil reads phi(i+3,j,j): y extents kept within the z extent)
+SHAPES = [(14, 11, 9), (7, 12, 16)]
 
 
 def _fields(g, seed, small):
@@ -62,6 +64,45 @@ def test_weno5_rhs(oracle, shape, small, spacing):
         outside = np.ones(phi.shape, bool)
         outside[fb[4]:fb[5] + 1, fb[2]:fb[3] + 1, fb[0]:fb[1] + 1] = False
         assert (rhs[outside] == 7.0).all()
+
+
+@pytest.mark.parametrize("scheme,name", [(2, "getrhs3d2nd_"), (3, "getrhs3d3rd_")])
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("small", [0.0, 0.3])
+def test_eno_rhs_variable(oracle, scheme, name, shape, small):
+    g = Q.make_grid(oracle, shape)
+    phi, vel, b, vx, vy, vz = _fields(g, 3 * sum(shape) + scheme, small)
+    dx, dy, dz = 0.04, 0.05, 0.03
+    for klo, khi in ((None, None), (g.klo_fb + 1, g.klo_fb + 3)):
+        rhs = np.full_like(phi, 7.0)
+        h = C.c_double(-5.0)
+        getattr(oracle, name)(Q.dptr(phi), Q.dptr(vel), Q.dptr(b), Q.dptr(vx), Q.dptr(vy), Q.dptr(vz), C.byref(h),
+                              Q.dptr(rhs), *Q.gb_args(g), *Q.fb_args(g, klo, khi), Q.dref(dx), Q.dref(dy),
+                              Q.dref(dz))
+        fb = _fb(g, klo, khi)
+        want, want_h = N.rhs_var(scheme, phi, vel, b, vx, vy, vz, fb, dx, dy, dz)
+        got = N._shift(rhs, fb)
+        assert np.array_equal(got, want), f"max |d| = {np.abs(got - want).max()}"
+        assert h.value == want_h
+
+
+@pytest.mark.parametrize("scheme,name", [(2, "getrhs3d2ndconst_"), (3, "getrhs3d3rdconst_")])
+@pytest.mark.parametrize("a", [1.3, -0.7, 4e-6])
+def test_eno_rhs_constant(oracle, scheme, name, a):
+    """Constant speed a (below the 1e-5 tolerance the normal term is never
+    set and stays 0) and curvature coefficient."""
+    g = Q.make_grid(oracle, SHAPES[0])
+    phi = _fields(g, 77, 0.0)[0]
+    dx, dy, dz = 0.04, 0.045, 0.035
+    rhs = np.full_like(phi, 7.0)
+    h = C.c_double(-5.0)
+    getattr(oracle, name)(Q.dptr(phi), Q.dref(a), Q.dref(0.04), C.byref(h), Q.dptr(rhs), *Q.gb_args(g),
+                          *Q.fb_args(g), Q.dref(dx), Q.dref(dy), Q.dref(dz))
+    fb = _fb(g)
+    want, want_h = N.rhs_const(scheme, phi, a, 0.04, fb, dx, dy, dz)
+    got = N._shift(rhs, fb)
+    assert np.array_equal(got, want), f"max |d| = {np.abs(got - want).max()}"
+    assert h.value == want_h
 
 
 def test_rk_stages(oracle):
