@@ -300,3 +300,170 @@ def signed_linear_extrapolation(phi, fb, face):
         idx[ax] = m
         phi[tuple(idx)] = pb + slope * dist
     return phi
+
+
+# ---------------------------------------------------------------------------
+# coefficients of the variable model, "util3d.f" = src/utilities/qss_util3d.f
+
+PI = 3.14159265358979323846
+ONE_OVER_PI = 0.31830988618379
+
+
+def _basic_heaviside(x):
+    """basicHeaviside (util3d.f:477-494): 0 below zero, 1 above, 1/2 at zero."""
+    return np.where(x < 0, 0.0, np.where(x > 0, 1.0, 0.5))
+
+
+def heaviside(x, eps, sin=np.sin):
+    """qssHeaviside (util3d.f:450-471); `sin` is the sine the caller's build
+    uses (the reference's libm, or the oracle's portable one)."""
+    v1 = _basic_heaviside(x + eps)
+    v2 = _basic_heaviside(eps - x)
+    v3 = _basic_heaviside(x - eps)
+    return (((0.5 + x / (2.0 * eps)) + (0.5 * ONE_OVER_PI) * sin((PI * x) / eps)) * v1) * v2 + v3
+
+
+def _mask_terms(mask, mx, my, mz, fb, dx, sin):
+    """h1, h2, |grad mask|, s of 3d.f:66-79 (the same text in 3d.f:150-163
+    and 3d.f:237-250)."""
+    m = _shift(mask, fb)
+    gx, gy, gz = _shift(mx, fb), _shift(my, fb), _shift(mz, fb)
+    eps_var = 1.5 * dx
+    h1 = heaviside(-m, eps_var, sin)
+    h2 = heaviside(m, eps_var, sin)
+    absgrad = np.sqrt((gx * gx + gy * gy) + gz * gz)
+    x = np.sqrt(m * m + ((absgrad * dx) * absgrad) * dx)
+    s = m / x
+    return h1, h2, absgrad, s, gx, gy, gz
+
+
+def set_var_norm(mask, mx, my, mz, a0, ca, fb, dx, sin=np.sin, cos=np.cos):
+    """setVarNorm3d (3d.f:13-87) with a scalar contact angle ca, or
+    setVarNorm3dTheta (3d.f:94-172) with ca an array: the normal speed over
+    the fill box, h1*a0 - s*h2*1*cos(ca)*|grad mask|."""
+    h1, h2, absgrad, s, *_ = _mask_terms(mask, mx, my, mz, fb, dx, sin)
+    c = cos(_shift(ca, fb)) if np.ndim(ca) else cos(np.full(h1.shape, float(ca)))
+    return h1 * a0 - (((s * h2) * 1.0) * c) * absgrad
+
+
+def set_var_curv_adv(mask, mx, my, mz, const_b, fb, dx, sin=np.sin):
+    """setVarCurvAdv3d (3d.f:178-298): curvature coefficient b = h1*const_b,
+    advection field s*1*grad mask*h2 and the two CFL bounds (true maxima,
+    -1 for an empty box): returns (b, vx, vy, vz, b_max_over_dx,
+    max_U_over_dx)."""
+    h1, h2, absgrad, s, gx, gy, gz = _mask_terms(mask, mx, my, mz, fb, dx, sin)
+    inv = 1.0 / dx
+    b = h1 * const_b
+    vx = ((s * 1.0) * gx) * h2
+    vy = ((s * 1.0) * gy) * h2
+    vz = ((s * 1.0) * gz) * h2
+    u = (np.abs(vx) * inv + np.abs(vy) * inv) + np.abs(vz) * inv
+    b_max = max(-1.0, float(b.max())) if b.size else -1.0
+    u_max = max(-1.0, float(u.max())) if u.size else -1.0
+    return b, vx, vy, vz, (2.0 * b_max) * ((inv * inv + inv * inv) + inv * inv), u_max
+
+
+def central_grad(phi, fb, dx, dy, dz):
+    """getCentralGrad3dOrder2 (3d.f:2987-3048) over the fill box."""
+    def s(di=0, dj=0, dk=0):
+        return _shift(phi, fb, di, dj, dk)
+
+    return ((s(1) - s(-1)) * (0.5 / dx), (s(0, 1) - s(0, -1)) * (0.5 / dy), (s(0, 0, 1) - s(0, 0, -1)) * (0.5 / dz))
+
+
+def impose_trap_velocity(mask_w, fields, fb, dx):
+    """imposeTrapVelocity3d (util3d.f:499-581), in place: the five fields
+    are zeroed on the fill box where the tested array exceeds 1.5*dx."""
+    sel = _shift(mask_w, fb) > 1.5 * dx
+    for f in fields:
+        _shift(f, fb)[sel] = 0.0
+    return fields
+
+
+def impose_mask(mask, phi, overlap, klo, khi):
+    """imposeMaskParallel (util3d.f:130-177; scalar overlap: max(mask -
+    overlap, phi)) and imposeMaskParallelVar (util3d.f:181-230; array
+    overlap: mask itself where mask - overlap > phi) on z-planes klo..khi of
+    the whole ghost box."""
+    m, p = mask[klo:khi + 1], phi[klo:khi + 1]
+    if np.ndim(overlap):
+        return np.where(m - overlap[klo:khi + 1] > p, m, p)
+    t = m - overlap
+    return np.where(t > p, t, p)
+
+
+def max_norm_diff_local(f1, f2, ib, zone):
+    """qss3dMaxNormDiffLocal (util3d.f:65-125): max |f1 - f2| where |f1| <
+    zone over the box ib, -1 when no voxel qualifies."""
+    a, b = _shift(f1, ib), _shift(f2, ib)
+    d = np.abs(a - b)[np.abs(a) < zone]
+    return max(-1.0, float(d.max())) if d.size else -1.0
+
+
+def volume_phi_less_than_zero(phi, ib, dx, dy, dz, eps, sin=np.sin):
+    """qss3dVolumeRegionPhiLessThanZero (util3d.f:288-359): the loop-order
+    sum of dV (phi < -eps) and (1 - H(phi))*dV (|phi| < eps), added one
+    voxel after the other in loop order (i fastest)."""
+    dV = (dx * dy) * dz
+    p = _shift(phi, ib).ravel()
+    x = p / eps
+    one_minus_h = 0.5 * ((1.0 - x) - ONE_OVER_PI * sin(PI * x))
+    c = np.where(p < -eps, dV, np.where(p < eps, one_minus_h * dV, 0.0))
+    return float(np.add.accumulate(np.concatenate(([0.0], c)))[-1])
+
+
+# ---------------------------------------------------------------------------
+# reinitialisation, "reinit3d.f" = src/reinitialization/qss_reinitialization3d.f
+
+def distance_for_subcell_fix(phi0, fb, dx, dy, dz):
+    """qss3dComputeDistanceForSubcellFix (reinit3d.f:476-580): phi0/delta at
+    voxels with a sign change to a face neighbour (delta the largest of the
+    one- and two-sided differences of the three axes and 1e-5), -1000*max
+    spacing elsewhere."""
+    def s(di=0, dj=0, dk=0):
+        return _shift(phi0, fb, di, dj, dk)
+
+    p = s()
+    near = np.zeros(p.shape, bool)
+    for o in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+        q = s(*o)
+        near |= ((q > 0.0) & (p <= 0.0)) | ((q <= 0.0) & (p > 0.0))
+    delta = np.full(p.shape, ZERO_TOL)
+    for d in range(3):
+        up, dn = s(*_axis(d, 1)), s(*_axis(d, -1))
+        d1 = np.abs(up - dn) / 2.0
+        d2 = np.abs(up - p)
+        d3 = np.abs(p - dn)
+        delta = np.maximum(np.maximum(np.maximum(d1, d2), d3), delta)
+    flag = -1000.0 * max(dx, dy, dz)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(near, p / delta, flag)
+
+
+def reinit_rhs_subcell_fix(phi, phi0, distance0, fb, dx, dy, dz):
+    """qss3dComputeReinitializationEqnRHSSubcellFixOrder1 (reinit3d.f:585-742)
+    over the fill box: first-order Godunov away from the interface (where
+    distance0 holds the flag), the Russo-Smereka subcell term
+    distance0 - sgn(phi0)*|phi|/max_dx next to it."""
+    def s(a, di=0, dj=0, dk=0):
+        return _shift(a, fb, di, dj, dk)
+
+    max_dx = max(dx, dy, dz)
+    flag = -1000.0 * max_dx
+    inv = (1.0 / dx, 1.0 / dy, 1.0 / dz)
+    p = s(phi)
+    p0 = s(phi0)
+    dist = s(distance0)
+    sgn = np.where(np.abs(p0) > ZERO_TOL, np.copysign(1.0, p0), 0.0)
+    pos = p > 0.0
+    g2 = None
+    for d in range(3):
+        plus = (s(phi, *_axis(d, 1)) - p) * inv[d]
+        minus = (p - s(phi, *_axis(d, -1))) * inv[d]
+        gp = np.where(pos, np.maximum(-plus, 0.0), np.maximum(plus, 0.0))
+        gm = np.where(pos, np.maximum(minus, 0.0), np.maximum(-minus, 0.0))
+        star = np.maximum(gp, gm)
+        g2 = star * star if g2 is None else g2 + star * star
+    away = np.where(np.abs(p) > ZERO_TOL, sgn - sgn * np.sqrt(g2), 0.0)
+    near = dist - (sgn * np.abs(p)) / max_dx
+    return np.where(dist == flag, away, near)
