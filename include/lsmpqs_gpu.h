@@ -194,6 +194,14 @@ void createIntersectionOfBoxes(QSSLIB_REAL *phi, int num_cuboids, QSSLIB_REAL *c
 void createBox(QSSLIB_REAL *phi, QSSLIB_REAL corner_x, QSSLIB_REAL corner_y, QSSLIB_REAL corner_z,
                QSSLIB_REAL side_length_x, QSSLIB_REAL side_length_y, QSSLIB_REAL side_length_z,
                int inside_flag, Grid *grid);
+/* src/geometry/qss_initialization2d.h:235-241, 277-284 (2-D circles, evaluated on the
+   host: the 2-D path is not on the GPU; createInitFromMask's 2-D branch calls
+   them) */
+void createIntersectionOfCircles(QSSLIB_REAL *phi, int num_circles, QSSLIB_REAL *center_x,
+                                 QSSLIB_REAL *center_y, QSSLIB_REAL *radius, int *inside_flag,
+                                 Grid *grid);
+void createCircle(QSSLIB_REAL *phi, QSSLIB_REAL center_x, QSSLIB_REAL center_y, QSSLIB_REAL radius,
+                  int inside_flag, Grid *grid);
 
 /* ---------------- GB300 extensions (no counterpart in the reference) ------- */
 /* error state: 0 = no error since the last clear */

@@ -10,6 +10,7 @@
 //   defaults         src/utilities/qss_options.c:42-117
 //   compression      src/utilities/qss_file.c:13-64 (gzip/bzip2 executables)
 #include <cctype>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -287,6 +288,34 @@ Grid* readGridFromBinaryFile(char* file_name) {
   }
   free(base);
   return g;
+}
+
+// ---------------------------------------------------------------- 2-D shapes
+// The 2-D initial shapes some reference tools call (createInitFromMask's
+// 2-D branch); host loops over the 2-D ghost box, as the reference
+// (src/geometry/qss_initialization2d.c:127-178): the larger of the signed
+// distances to the circles, each negated when its inside_flag is >= 0.
+void createIntersectionOfCircles(QSSLIB_REAL* phi, int num_circles, QSSLIB_REAL* center_x, QSSLIB_REAL* center_y,
+                                 QSSLIB_REAL* radius, int* inside_flag, Grid* grid) {
+  const int nx = grid->grid_dims_ghostbox[0], ny = grid->grid_dims_ghostbox[1];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      const double x = grid->x_lo_ghostbox[0] + grid->dx[0] * i;
+      const double y = grid->x_lo_ghostbox[1] + grid->dx[1] * j;
+      double best = -FLT_MAX;
+      for (int c = 0; c < num_circles; c++) {
+        const double ex = x - center_x[c], ey = y - center_y[c];
+        double d = sqrt(ex * ex + ey * ey) - radius[c];
+        if (inside_flag[c] >= 0) d = -d;
+        if (d > best) best = d;
+      }
+      phi[i + j * nx] = best;
+    }
+}
+
+void createCircle(QSSLIB_REAL* phi, QSSLIB_REAL center_x, QSSLIB_REAL center_y, QSSLIB_REAL radius, int inside_flag,
+                  Grid* grid) {
+  createIntersectionOfCircles(phi, 1, &center_x, &center_y, &radius, &inside_flag, grid);
 }
 
 // ---------------------------------------------------------------- data arrays
