@@ -310,31 +310,33 @@ def _e2e_call(lib, g, mask, phi, steps, dist, pinned=False):
         raw = (C.c_ubyte * nbytes).from_address(ptr)
         return np.frombuffer(raw, dtype=dtype).reshape(shape)
 
-    w = Q.Volume(g, alloc=pinned_zeros if pinned else None)
-    w["mask"][...] = mask
-    w["phi"][...] = phi
-    o = Q.default_options(lib)
-    set_options(lib, o)
-    _fill_host_coefficients(lib, o, w, o.a)
-    dt_est = 0.5 / (o.b_max_over_dx + o.max_U_over_dx)
-    o.tplot = steps * dt_est * 0.999
-    o.tmax = o.tplot * 0.5
-    o.use_satn_stop = 0
-    dist.barrier()
-    t0 = time.perf_counter()
-    lib.constCurvModel3d(C.byref(o), C.byref(w.p), C.byref(g), None)
-    t1 = time.perf_counter()
-    Q.check(lib)
-    steps_done, outer = C.c_longlong(0), C.c_longlong(0)
-    lib.qssgpu_call_stats(C.byref(w.p), C.byref(g), C.byref(steps_done), C.byref(outer))
-    ph = (C.c_double * 8)()
-    lib.qssgpu_call_times(C.byref(w.p), C.byref(g), ph)
-    lib.qssgpu_release(C.byref(w.p))
-    res = {"wall": dist.max(t1 - t0), "steps": steps_done.value, "outer": outer.value,
-            "phases": {k: round(ph[i], 3) for i, k in enumerate(PHASES) if k not in ("total", "setup")}}
-    del w
-    for ptr in buffers:
-        lib.qssgpu_host_free(ptr)
+    try:
+        w = Q.Volume(g, alloc=pinned_zeros if pinned else None)
+        w["mask"][...] = mask
+        w["phi"][...] = phi
+        o = Q.default_options(lib)
+        set_options(lib, o)
+        _fill_host_coefficients(lib, o, w, o.a)
+        dt_est = 0.5 / (o.b_max_over_dx + o.max_U_over_dx)
+        o.tplot = steps * dt_est * 0.999
+        o.tmax = o.tplot * 0.5
+        o.use_satn_stop = 0
+        dist.barrier()
+        t0 = time.perf_counter()
+        lib.constCurvModel3d(C.byref(o), C.byref(w.p), C.byref(g), None)
+        t1 = time.perf_counter()
+        Q.check(lib)
+        steps_done, outer = C.c_longlong(0), C.c_longlong(0)
+        lib.qssgpu_call_stats(C.byref(w.p), C.byref(g), C.byref(steps_done), C.byref(outer))
+        ph = (C.c_double * 8)()
+        lib.qssgpu_call_times(C.byref(w.p), C.byref(g), ph)
+        lib.qssgpu_release(C.byref(w.p))
+        res = {"wall": dist.max(t1 - t0), "steps": steps_done.value, "outer": outer.value,
+                "phases": {k: round(ph[i], 3) for i, k in enumerate(PHASES) if k not in ("total", "setup")}}
+    finally:
+        # the page-locked buffers go back even when the call failed
+        for ptr in buffers:
+            lib.qssgpu_host_free(ptr)
     return res
 
 
