@@ -241,6 +241,15 @@ int qssgpu_set_axis_variant(int variant);
 int qssgpu_axis_tuning(int* rows, int max_rows);
 /* forgets the tuned launch shapes */
 void qssgpu_axis_tuning_reset(void);
+/* writes the tuned launch shapes to a text file, one shape a line (the 7
+   numbers of qssgpu_axis_tuning); returns the number written, -1 on error */
+int qssgpu_axis_tuning_save(const char *path);
+/* adds the shapes of such a file to the table (a shape already there keeps
+   its pick), so later processes skip the timing; every line is checked first
+   (level 1-2, axis 0-2, positive sizes, form 0/1, 1 <= segment length <= line
+   length) and a file with any other line adds nothing; returns the number of
+   shapes read, -1 on error */
+int qssgpu_axis_tuning_load(const char *path);
 /* Batched mode (no reference counterpart): the curvature ladder of
    drain_model3d (drain != 0) or imbibe_model3d on n independent volumes at
    once, each with its own Options (contact angle, curvature ladder), arrays

@@ -30,6 +30,7 @@
 //   E(c) = 1/4 (v(c+1) - v(c-1))^2              second term of S2+(c-1) and S2-(c)
 //   eps-(i) = eps+(i-1)                          (same five squares, max is exact)
 #include <array>
+#include <cstdio>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -722,6 +723,48 @@ int qssgpu_axis_tuning(int* rows, int max_rows) {
 void qssgpu_axis_tuning_reset(void) {
   std::lock_guard<std::mutex> lk(qss::g_tune_mu);
   qss::g_tune.clear();
+}
+
+int qssgpu_axis_tuning_save(const char* path) {
+  if (!path) return -1;
+  FILE* fp = fopen(path, "w");
+  if (!fp) return -1;
+  std::lock_guard<std::mutex> lk(qss::g_tune_mu);
+  int n = 0;
+  fprintf(fp, "# level axis lanes lines_per_lane line form seg_len\n");
+  for (const auto& kv : qss::g_tune) {
+    fprintf(fp, "%d %d %d %d %d %d %d\n", kv.first[0], kv.first[1], kv.first[2], kv.first[3], kv.first[4],
+            kv.second[0], kv.second[1]);
+    n++;
+  }
+  return fclose(fp) == 0 ? n : -1;
+}
+
+int qssgpu_axis_tuning_load(const char* path) {
+  if (!path) return -1;
+  FILE* fp = fopen(path, "r");
+  if (!fp) return -1;
+  // every row is checked before any is added: a launch shape from the file
+  // must be one the tuner itself could have picked
+  std::vector<std::pair<qss::TuneKey, std::array<int, 2>>> rows;
+  char line[256];
+  bool ok = true;
+  while (ok && fgets(line, sizeof line, fp)) {
+    const char* c = line;
+    while (*c == ' ' || *c == '\t') c++;
+    if (*c == '#' || *c == '\n' || *c == 0) continue;
+    int v[7];
+    char tail;
+    ok = sscanf(c, "%d %d %d %d %d %d %d %c", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &tail) == 7 &&
+         v[0] >= 1 && v[0] <= 2 && v[1] >= 0 && v[1] <= 2 && v[2] > 0 && v[3] > 0 && v[4] > 0 &&
+         (v[5] == 0 || v[5] == 1) && v[6] >= 1 && v[6] <= v[4];
+    if (ok) rows.push_back({qss::TuneKey{v[0], v[1], v[2], v[3], v[4]}, std::array<int, 2>{v[5], v[6]}});
+  }
+  fclose(fp);
+  if (!ok) return -1;
+  std::lock_guard<std::mutex> lk(qss::g_tune_mu);
+  for (const auto& r : rows) qss::g_tune.emplace(r.first, r.second);
+  return (int)rows.size();
 }
 
 }  // extern "C"

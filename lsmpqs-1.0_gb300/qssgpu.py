@@ -166,6 +166,8 @@ def load(path: str) -> C.CDLL:
         "qssgpu_set_axis_variant": (C.c_int, [C.c_int]),
         "qssgpu_axis_tuning": (C.c_int, [C.POINTER(C.c_int), C.c_int]),
         "qssgpu_axis_tuning_reset": (None, []),
+        "qssgpu_axis_tuning_save": (C.c_int, [C.c_char_p]),
+        "qssgpu_axis_tuning_load": (C.c_int, [C.c_char_p]),
         "qssgpu_host_alloc": (C.c_void_p, [C.c_size_t]),
         "qssgpu_host_free": (None, [C.c_void_p]),
         "qssgpu_call_times": (None, [P(QSSDataArrays), P(Grid), P(C.c_double)]),

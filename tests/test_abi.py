@@ -131,3 +131,39 @@ def test_axis_variant_settings(lib):
         L.qssgpu_set_axis_variant(prev)
     L.qssgpu_axis_tuning_reset()
     assert L.qssgpu_axis_tuning(None, 0) == 0
+
+
+def test_axis_tuning_file_round_trip(lib, tmp_path):
+    """Tuned launch shapes saved to a file and loaded back (no GPU needed):
+    valid rows are added, a shape already in the table keeps its pick, and a
+    file with any invalid row (a segment length of 0 or longer than the line,
+    an unknown form, a bad level or axis, a short row) adds nothing."""
+    L = Q.load(Q.GPU_LIB)
+    L.qssgpu_axis_tuning_reset()
+    good = tmp_path / "shapes"
+    good.write_text("# level axis lanes lines_per_lane line form seg_len\n"
+                    "2 0 512 512 512 1 128\n2 1 512 512 512 1 128\n\n  2 2 512 512 512 0 16\n")
+    assert L.qssgpu_axis_tuning_load(str(good).encode()) == 3
+    rows = (C.c_int * 21)()
+    assert L.qssgpu_axis_tuning(rows, 7) == 3
+    got = sorted(tuple(rows[7 * i:7 * i + 7]) for i in range(3))
+    assert got == [(2, 0, 512, 512, 512, 1, 128), (2, 1, 512, 512, 512, 1, 128), (2, 2, 512, 512, 512, 0, 16)]
+    # the first pick of a shape stays
+    other = tmp_path / "other"
+    other.write_text("2 0 512 512 512 0 64\n1 0 40 40 40 0 20\n")
+    assert L.qssgpu_axis_tuning_load(str(other).encode()) == 2
+    assert L.qssgpu_axis_tuning(None, 0) == 4
+    back = tmp_path / "saved"
+    assert L.qssgpu_axis_tuning_save(str(back).encode()) == 4
+    assert "2 0 512 512 512 1 128" in back.read_text()
+    assert "2 0 512 512 512 0 64" not in back.read_text()
+    for bad in ("2 0 512 512 512 1 0", "2 0 512 512 512 1 513", "2 0 512 512 512 2 64", "3 0 8 8 8 0 8",
+                "2 3 8 8 8 0 8", "2 0 8 8 8 0", "2 0 8 8 8 0 8 9", "2 0 -8 8 8 0 8"):
+        f = tmp_path / "bad"
+        f.write_text("2 1 64 64 64 0 16\n" + bad + "\n")
+        assert L.qssgpu_axis_tuning_load(str(f).encode()) == -1, bad
+    assert L.qssgpu_axis_tuning(None, 0) == 4
+    assert L.qssgpu_axis_tuning_load(str(tmp_path / "missing").encode()) == -1
+    L.qssgpu_axis_tuning_reset()
+    assert L.qssgpu_axis_tuning_load(str(back).encode()) == 4
+    L.qssgpu_axis_tuning_reset()
