@@ -245,7 +245,8 @@ void qssgpu_axis_tuning_reset(void);
    numbers of qssgpu_axis_tuning); returns the number written, -1 on error */
 int qssgpu_axis_tuning_save(const char *path);
 /* adds the shapes of such a file to the table (a shape already there keeps
-   its pick), so later processes skip the timing; every line is checked first
+   its pick), so later processes in tuned mode (axis variant 2) skip the
+   timing of those shapes; every line is checked first
    (level 1-2, axis 0-2, positive sizes, form 0/1, 1 <= segment length <= line
    length) and a file with any other line adds nothing; returns the number of
    shapes read, -1 on error */
