@@ -99,7 +99,7 @@ int main(int argc, char** argv) {
   g_jitter = argc > 3 ? atoi(argv[3]) : 0;
   long long fam1 = 0;
   Count c_sqrt{"sqrt"}, c_div{"div"}, c_mul{"mul"}, c_add{"add"}, c_sub{"sub"}, c_sc{"scale2"}, c_cmp{"compare"},
-      c_max{"max_nonneg"};
+      c_max{"max_nonneg"}, c_sign{"neg_abs"};
   int shown = 0;
   auto report = [&](const char* op, double x, double y, double got, double want) {
     if (shown++ < 12)
@@ -127,6 +127,10 @@ int main(int argc, char** argv) {
     g = qss_emu::sub(x, y), w = x - y;
     c_sub.n++;
     if (!same(g, w)) c_sub.bad++, report("sub", x, y, g, w);
+    // sign flip and magnitude: bit for bit, NaN sign bits included
+    c_sign.n++;
+    if (bts(qss_emu::neg(x)) != bts(-x) || bts(qss_emu::abs(x)) != bts(std::fabs(x)))
+      c_sign.bad++, report("neg_abs", x, 0, qss_emu::neg(x), -x);
     const int k = (int)(rnd() % 9) - 4;
     g = qss_emu::scale2(x, k), w = x * std::ldexp(1.0, k);
     c_sc.n++;
@@ -154,7 +158,7 @@ int main(int argc, char** argv) {
   }
   printf("sqrt_positive %lld %lld\n", sq_pos, g_fallback[3] - fb0);
   long long bad = 0;
-  for (const Count* c : {&c_sqrt, &c_div, &c_mul, &c_add, &c_sub, &c_sc, &c_cmp, &c_max}) {
+  for (const Count* c : {&c_sqrt, &c_div, &c_mul, &c_add, &c_sub, &c_sc, &c_cmp, &c_max, &c_sign}) {
     printf("%s %lld %lld\n", c->name, c->n, c->bad);
     bad += c->bad;
   }

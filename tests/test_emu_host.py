@@ -27,7 +27,8 @@ def _run(exe, cases, seed, jitter):
     rows = {}
     for line in r.stdout.splitlines():
         f = line.split()
-        if len(f) >= 3 and f[0] in ("sqrt", "div", "mul", "add", "sub", "scale2", "compare", "max_nonneg"):
+        if len(f) >= 3 and f[0] in ("sqrt", "div", "mul", "add", "sub", "scale2", "compare", "max_nonneg",
+                                     "neg_abs"):
             rows[f[0]] = (int(f[1]), int(f[2]))
         if f and f[0] == "fallbacks_normal":
             rows["fallbacks"] = tuple(int(x) for x in f[1:])
@@ -40,7 +41,7 @@ def _run(exe, cases, seed, jitter):
 def test_emulated_ops_bit_exact(checker, seed, jitter):
     rc, rows, out = _run(checker, 2_000_000, seed, jitter)
     assert rc == 0, out
-    for op in ("sqrt", "div", "mul", "add", "sub", "scale2", "compare", "max_nonneg"):
+    for op in ("sqrt", "div", "mul", "add", "sub", "scale2", "compare", "max_nonneg", "neg_abs"):
         n, bad = rows[op]
         assert n > 1_000_000 and bad == 0, out
     # normal operands take the integer path (no native fallback)
