@@ -100,6 +100,26 @@ def test_union_find_labels_are_component_maxima(oracle):
     assert int(lab.sum()) == 2 * flat(4, 4, 4) + flat(5, 5, 9)
 
 
+@pytest.mark.parametrize("density", [0.2, 0.35, 0.6])
+def test_union_find_matches_scipy_components(oracle, density):
+    """Labels are independent of the order of the unions: on random binaries
+    every 26-connected component (scipy's labelling, computed without any
+    union-find) carries its largest linear index, background 0."""
+    ndimage = pytest.importorskip("scipy.ndimage")
+    g = _grid(oracle, (13, 9, 11))
+    v = Q.Volume(g)
+    rng = np.random.default_rng(int(100 * density))
+    b = (rng.random(v.shape) < density).astype(np.uint8)
+    v["phi_bin"][...] = b
+    oracle.findConnectivity3d(C.byref(v.p), C.byref(g))
+    comp, n = ndimage.label(b, structure=np.ones((3, 3, 3), int))
+    flat = np.arange(b.size).reshape(b.shape)
+    top = np.zeros(n + 1, np.int64)
+    np.maximum.at(top, comp.ravel(), flat.ravel())
+    want = np.where(comp > 0, top[comp], 0)
+    assert np.array_equal(v["connectivity"], want)
+
+
 def test_portable_sine_is_accurate(oracle):
     xs = np.linspace(-3.3, 3.3, 20001)
     s = np.array([oracle.oracle_portable_sin(float(x)) for x in xs])
