@@ -27,10 +27,13 @@ def _both(ref, oracle, fn, threads=1):
     return out
 
 
-@pytest.mark.parametrize("theta,space,time,threads", [
-    (0, 2, 2, 1), (0, 3, 3, 2), (0, 5, 1, 3), (10, 2, 2, 1), (30, 5, 3, 4), (40, 3, 3, 1), (60, 5, 3, 2)])
-def test_drain_imbibe_drivers(ref, oracle, theta, space, time, threads):
-    g, v = pack_case(oracle, 20, seed=theta + space)
+@pytest.mark.parametrize("theta,space,time,threads,n", [
+    (0, 2, 2, 1, 20), (0, 3, 3, 2, 20), (0, 5, 1, 3, 20), (10, 2, 2, 1, 20), (30, 5, 3, 4, 20), (40, 3, 3, 1, 20),
+    (60, 5, 3, 2, 20),
+    # non-cubic fill boxes (the ENO3 x stencil's phi(i+3,j,j) needs y within z)
+    (10, 5, 3, 3, (19, 13, 16)), (0, 2, 2, 2, (15, 18, 12)), (20, 3, 3, 2, (14, 11, 17))])
+def test_drain_imbibe_drivers(ref, oracle, theta, space, time, threads, n):
+    g, v = pack_case(oracle, n, seed=theta + space)
 
     def run(lib):
         w = clone(v)
