@@ -47,7 +47,7 @@ def _axis(d, m):
 
 
 def weno5_side(v1, v2, v3, v4, v5):
-    """HJ WENO5 reconstruction from five scaled differences (3d.f:1981-2014)."""
+    """HJ WENO5 reconstruction from five scaled differences (3d.f:1976-2005)."""
     eps = 1e-6 * np.maximum(np.maximum(np.maximum(np.maximum(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5) + TINY
     p1 = (C13 * v1 - C76 * v2) + C116 * v3
     p2 = (-(C16 * v2) + C56 * v3) + C13 * v4
@@ -71,7 +71,7 @@ def weno5_side(v1, v2, v3, v4, v5):
 
 
 def weno5_plus_minus(phi, fb, d, inv):
-    """phi_plus and phi_minus along axis d (3d.f:1969-2247): faces
+    """phi_plus and phi_minus along axis d (3d.f:1962-2250): faces
     D(m) = phi(i+m) - phi(i+m-1), scaled by 1/dx."""
     D = {m: _shift(phi, fb, *_axis(d, m)) - _shift(phi, fb, *_axis(d, m - 1)) for m in range(-2, 4)}
     plus = weno5_side(D[3] * inv, D[2] * inv, D[1] * inv, D[0] * inv, D[-1] * inv)
@@ -80,8 +80,8 @@ def weno5_plus_minus(phi, fb, d, inv):
 
 
 def eno2_plus_minus(phi, fb, d, inv):
-    """ENO2 phi_plus and phi_minus along axis d (3d.f:1113-1182, the same
-    text in the constant-coefficient variant 3d.f:394-463): second
+    """ENO2 phi_plus and phi_minus along axis d (3d.f:1119-1190, the same
+    text in the constant-coefficient variant 3d.f:387-458): second
     differences taken from phi directly, the smaller one in magnitude
     chosen (ties take the second)."""
     def s(m):
@@ -98,11 +98,11 @@ def eno2_plus_minus(phi, fb, d, inv):
 
 
 def eno3_plus_minus(phi, fb, d, inv, inv_minus):
-    """ENO3 phi_plus and phi_minus along axis d (3d.f:1446-1700, the same
-    text in the constant-coefficient variant 3d.f:676-931).  Kept as the
+    """ENO3 phi_plus and phi_minus along axis d (3d.f:1449-1680, the same
+    text in the constant-coefficient variant 3d.f:672-903).  Kept as the
     Fortran has them: the x stencil's outermost plus point is phi(i+3,j,j)
     (3d.f:1454), and the y and z minus derivatives are scaled by 1/dx
-    (inv_minus = 1/dx for every axis)."""
+    (3d.f:1600, 1677; inv_minus = 1/dx for every axis)."""
     def s(m):
         return _shift(phi, fb, *_axis(d, m))
 
@@ -149,9 +149,10 @@ def _sq(x):
 
 
 def _assemble(pm, phi, vn, b, adv, fb, dx, dy, dz, norm_sign):
-    """The part every right-hand-side variant shares (3d.f:2249-2385 for
-    WENO5; the same text for ENO2 3d.f:1183-1320 and ENO3 3d.f:1701-1812,
-    and without the advection term for the constant-coefficient variants):
+    """The part every right-hand-side variant shares (3d.f:2251-2379 for
+    WENO5; the same text for ENO2 3d.f:1191-1319 and ENO3 3d.f:1681-1809,
+    and without the advection term for the constant-coefficient variants
+    3d.f:459-560 and 904-1004):
     Godunov normal term (sign +1 for WENO5, -1 otherwise), CFL estimate of
     the last voxel, upwind advection (adv = (vx, vy, vz) or None), central
     curvature.  vn and b are arrays over the fill box."""
@@ -250,7 +251,7 @@ def rhs_var(scheme, phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
 
 
 def rhs_weno5(phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz):
-    """getRHS3d5th (3d.f:1827-2385), see rhs_var."""
+    """getRHS3d5th (3d.f:1827-2386), see rhs_var."""
     return rhs_var(5, phi, vel_n, b, vx, vy, vz, fb, dx, dy, dz)
 
 
@@ -324,8 +325,8 @@ def heaviside(x, eps, sin=np.sin):
 
 
 def _mask_terms(mask, mx, my, mz, fb, dx, sin):
-    """h1, h2, |grad mask|, s of 3d.f:66-79 (the same text in 3d.f:150-163
-    and 3d.f:237-250)."""
+    """h1, h2, |grad mask|, s of 3d.f:72-80 (the same text in 3d.f:156-164
+    and 3d.f:263-271)."""
     m = _shift(mask, fb)
     gx, gy, gz = _shift(mx, fb), _shift(my, fb), _shift(mz, fb)
     eps_var = 1.5 * dx
