@@ -161,7 +161,7 @@ void setvarcurvadv3d_(const double *mask, const double *mask_x, const double *ma
 /* Upwind one-sided derivatives.  Each helper returns (plus, minus) for one
    direction at one voxel, written exactly as the Fortran statements. */
 
-/* HJ ENO2 (3d.f:386-455): st[0..4] = phi at offsets -2..+2 along the axis */
+/* HJ ENO2 (3d.f:387-458): st[0..4] = phi at offsets -2..+2 along the axis */
 static void eno2_pm(const double st[5], double inv, double *plus, double *minus)
 {
   const double half = 0.5;
@@ -176,7 +176,7 @@ static void eno2_pm(const double st[5], double inv, double *plus, double *minus)
   else                        *minus = (D1 + half * D2) * inv;
 }
 
-/* HJ ENO3 (3d.f:665-925): st[0..6] = phi at offsets -3..+3; the caller
+/* HJ ENO3 (3d.f:672-903): st[0..6] = phi at offsets -3..+3; the caller
    substitutes the off-plane value for st[6] to keep the x typo, and passes
    inv_plus / inv_minus separately to keep the inv_dx scaling quirk. */
 static void eno3_pm(const double st[7], double inv_plus, double inv_minus,
@@ -222,7 +222,7 @@ static void eno3_pm(const double st[7], double inv_plus, double inv_minus,
   *minus = m * inv_minus;
 }
 
-/* HJ WENO5 weights and reconstruction for one side (3d.f:1981-2014) */
+/* HJ WENO5 weights and reconstruction for one side (3d.f:1976-2005) */
 static double weno5_side(double v1, double v2, double v3, double v4, double v5)
 {
   const double tiny_nonzero_number = 1.0e-35;
@@ -253,7 +253,7 @@ static double weno5_side(double v1, double v2, double v3, double v4, double v5)
   return a1 * p1 + a2 * p2 + a3 * p3;
 }
 
-/* st[0..6] = phi at offsets -3..+3 along the axis (3d.f:1968-2027) */
+/* st[0..6] = phi at offsets -3..+3 along the axis (3d.f:1962-2049) */
 static void weno5_pm(const double st[7], double inv, double *plus, double *minus)
 {
   double D1 = st[3] - st[2];
