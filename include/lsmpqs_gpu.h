@@ -232,7 +232,7 @@ int qssgpu_set_emu_level(int level);
    over each line shape times every distinct (form, segment length) and the
    fastest is kept for that shape (one stream synchronisation per new shape
    and axis); identical results; returns the previous setting.  No
-   reference counterpart: the reference's getrhs3d5th_ (3d.f:1968-2138) is a
+   reference counterpart: the reference's getrhs3d5th_ (3d.f:1962-2246) is a
    loop over voxels with nothing to tune. */
 int qssgpu_set_axis_variant(int variant);
 /* the launch shapes chosen in tuned mode so far: at most max_rows rows of 7

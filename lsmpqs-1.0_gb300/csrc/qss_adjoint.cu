@@ -46,7 +46,7 @@ namespace {
 constexpr double kC13 = 1.0 / 3.0, kC76 = 7.0 / 6.0, kC116 = 11.0 / 6.0, kC16 = 1.0 / 6.0, kC56 = 5.0 / 6.0;
 constexpr double k1312 = 13.0 / 12.0, k136 = 13.0 / 6.0;
 
-// Godunov term of WENO5 (3d.f:2245-2276) and its partials: dtn/d(pp, pm), dtn/dvel
+// Godunov term of WENO5 (3d.f:2251-2276) and its partials: dtn/d(pp, pm), dtn/dvel
 __device__ __forceinline__ double godunov_bwd(double vel, const double pp[3], const double pm[3], double ppb[3],
                                               double pmb[3], double& velb) {
   double a[3], c[3];
@@ -101,7 +101,7 @@ struct AdjPointArgs {
 
 // Per fill-box voxel: the adjoints of the six one-sided WENO5 derivatives
 // (Godunov normal term and upwind advection) and the partials of the
-// curvature term b kappa (3d.f:2336-2378) with respect to its ten central
+// curvature term b kappa (3d.f:2337-2379) with respect to its ten central
 // differences, each times the voxel's adjoint weight.  Voxels whose normal
 // term is carried from an earlier voxel leave that term to k_adj_carry.
 __global__ void __launch_bounds__(128) k_adj_point(AdjPointArgs a) {
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(128) k_adj_point(AdjPointArgs a) {
       const double pyz = (phi[q + st[1] + st[2]] + phi[q - st[1] - st[2]] - phi[q - st[1] + st[2]] -
                           phi[q + st[1] - st[2]]) * a.f2[5];
       const double sx = phx * phx, sy = phy * phy, sz = phz * phz;
-      // kappa numerator (3d.f:2336-2378), regrouped
+      // kappa numerator (3d.f:2337-2379), regrouped
       const double curv = pxx * (sy + sz) + pyy * (sx + sz) + pzz * (sx + sy) -
                           2 * (pxy * phx * phy + pxz * phx * phz + pyz * phy * phz);
       const double ig = qss_emu::div(1.0, grad);
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(128) k_adj_carry(AdjPointArgs a) {
   }
 }
 
-// Reverse of the WENO5 one-sided derivatives along one axis (3d.f:1968-2138),
+// Reverse of the WENO5 one-sided derivatives along one axis (3d.f:1962-2246),
 // one face window at a time.  With v(m) = (phi(m) - phi(m-1)) inv the scaled
 // difference of face m, the minus derivative of voxel c and the plus
 // derivative of voxel c-1 are the same WENO5 reconstruction of the window

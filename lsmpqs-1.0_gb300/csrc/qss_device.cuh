@@ -89,7 +89,7 @@ __device__ __forceinline__ double qss_heaviside(double x, double eps) {
 // ---------------------------------------------------------------------------
 // One-sided derivatives along one axis.  s[] holds phi at offsets -R..+R.
 
-// HJ ENO2, 3d.f:386-455 (R = 2)
+// HJ ENO2, 3d.f:387-458 (R = 2)
 __device__ __forceinline__ void eno2_pm(const double s[5], double inv, double& plus, double& minus) {
   const double half = 0.5;
   double D1 = s[2] - s[1];
@@ -101,7 +101,7 @@ __device__ __forceinline__ void eno2_pm(const double s[5], double inv, double& p
   minus = (fabs(D2m) < fabs(D2)) ? (D1 + half * D2m) * inv : (D1 + half * D2) * inv;
 }
 
-// HJ ENO3, 3d.f:665-925 (R = 3); the y/z minus derivatives are scaled by
+// HJ ENO3, 3d.f:672-903 (R = 3); the y/z minus derivatives are scaled by
 // inv_dx in the reference, so the two scalings are passed separately.
 __device__ __forceinline__ void eno3_pm(const double s[7], double inv_p, double inv_m, double& plus,
                                         double& minus) {
@@ -130,7 +130,7 @@ __device__ __forceinline__ void eno3_pm(const double s[7], double inv_p, double 
   minus = m * inv_m;
 }
 
-// HJ WENO5 weights and reconstruction of one side, 3d.f:1981-2014
+// HJ WENO5 weights and reconstruction of one side, 3d.f:1976-2005
 __device__ __forceinline__ double weno5_side(double v1, double v2, double v3, double v4, double v5) {
   const double tiny_nonzero_number = 1.0e-35;
   const double one_third = 1.0 / 3.0, seven_sixths = 7.0 / 6.0, eleven_sixths = 11.0 / 6.0;
@@ -159,7 +159,7 @@ __device__ __forceinline__ double weno5_side(double v1, double v2, double v3, do
   return a1 * p1 + a2 * p2 + a3 * p3;
 }
 
-// 3d.f:1968-2027 (R = 3)
+// 3d.f:1962-2049 (R = 3)
 __device__ __forceinline__ void weno5_pm(const double s[7], double inv, double& plus, double& minus) {
   double D1 = s[3] - s[2], D1p = s[4] - s[3], D1m = s[2] - s[1];
   double D1pp = s[5] - s[4], D1ppp = s[6] - s[5], D1mm = s[1] - s[0];
@@ -245,7 +245,7 @@ struct Fac {
 };
 
 // Central curvature term b*kappa|grad phi| with 2-cell second differences
-// (3d.f:2336-2378)
+// (3d.f:2337-2379)
 __device__ __forceinline__ double curvature(const double* __restrict__ phi, const Box& b, int64_t c,
                                             const Fac& f) {
   const int64_t sy = b.sy(), sz = b.sz();

@@ -2,7 +2,7 @@
 // sub-expressions.
 //
 // The reference evaluates, for every voxel and axis, two WENO5 reconstructions
-// from ten scaled first differences (3d.f:1968-2138).  Most of that work
+// from ten scaled first differences (3d.f:1962-2246).  Most of that work
 // depends only on one cell face or one cell centre and is therefore repeated
 // by up to six neighbouring voxels: the scaled difference v of a face, its
 // square, its multiples by 3 and by the five stencil coefficients, and the
@@ -156,7 +156,7 @@ __device__ __forceinline__ double eps_of(double w1, double w2, double w3, double
   return 1e-6 * m + 1.0e-35;
 }
 
-// weights and combination of one side (3d.f:1999-2014) given the candidate
+// weights and combination of one side (3d.f:1996-2005) given the candidate
 // stencils and smoothness indicators
 template <int EMU, bool SQ>
 __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, double S1, double S2, double S3,
@@ -365,7 +365,7 @@ struct CombineArgs {
   const Ctl* ctl;
 };
 
-// Godunov normal term of the WENO5 scheme, vel * |grad| (3d.f:2245-2276),
+// Godunov normal term of the WENO5 scheme, vel * |grad| (3d.f:2251-2276),
 // with the sign tests and maxima on the integer pipes at EMU >= 1
 template <int EMU>
 __device__ __forceinline__ double godunov5(double vel, const double pp[3], const double pm[3]) {
@@ -398,7 +398,7 @@ __device__ __forceinline__ bool speed_valid(double v) {
   return a >= qss_emu::bits(1.e-5) && a <= 0x7ff0000000000000ull;
 }
 
-// central curvature term (3d.f:2336-2378), same operations as curvature()
+// central curvature term (3d.f:2337-2379), same operations as curvature()
 // with the exact doublings, the threshold test and the division moved to the
 // integer pipes at EMU >= 1
 template <int EMU>
