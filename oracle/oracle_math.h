@@ -3,8 +3,8 @@
  * the oracle's restatement of the smoothed Heaviside and the volume integral.
  *
  * The reference evaluates SIN/COS through the platform libm (Fortran
- * intrinsics in src/utilities/qss_util3d.f:334-336, 461-462 and
- * src/spatial_derivatives/qss_spatial_derivatives3d.f:82).  libm results
+ * intrinsics in src/utilities/qss_util3d.f:346-348, 466-467 and
+ * src/spatial_derivatives/qss_spatial_derivatives3d.f:81, 166).  libm results
  * differ in the last bit between x86-64 and aarch64 builds and from any GPU
  * implementation, which would make bit-exact parity impossible.  Both the
  * oracle and the GPU kernels therefore evaluate sine with the same published
