@@ -155,6 +155,40 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class ResultLine:
+    """Keeps fd 1 for the one JSON result line.
+
+    The library mirrors the reference's printf progress lines
+    (constCurvModel3d.c:316-323, drain_model3d.c:104); libc buffers them
+    separately from Python's sys.stdout and flushes them at exit, after any
+    line printed from Python.  While the arms run, fd 1 points at fd 2, so
+    every C and Python write goes to stderr; emit() flushes both buffers,
+    restores fd 1 and prints the line as the last write to stdout."""
+
+    def __init__(self):
+        self._libc = C.CDLL(None)
+        sys.stdout.flush()
+        self._saved = os.dup(1)
+        os.dup2(2, 1)
+
+    def _flush(self):
+        self._libc.fflush(None)
+        sys.stdout.flush()
+        sys.stderr.flush()
+
+    def emit(self, line: dict | None):
+        self._flush()
+        os.dup2(self._saved, 1)
+        os.close(self._saved)
+        self._saved = None
+        if line is not None:
+            print(json.dumps(line), flush=True)
+
+    def close(self):
+        if self._saved is not None:
+            self.emit(None)
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -243,8 +277,13 @@ def gpu_arm(args, dist: Dist):
         npts = g.num_gridpts
         h2d = 8 * npts * len(E2E_FROM_HOST)
         d2h = 8 * npts * 5 + 4 * npts + npts  # phi, phi_next, phi_prev, mask_w, mask_nw, labels, phi_bin
-        e2e = {"value": dist.ws * nvox * r["steps"] / r["wall"], "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "inner_steps": r["steps"], "outer_iterations": r["outer"],
+        # the call copies its arrays once in each direction for all its
+        # inner steps: per step is the call's bytes over its inner steps
+        e2e = {"value": dist.ws * nvox * r["steps"] / r["wall"], "unit": UNIT,
+               "h2d_bytes_per_step": round(h2d / max(r["steps"], 1)),
+               "d2h_bytes_per_step": round(d2h / max(r["steps"], 1)),
+               "h2d_bytes_per_call": h2d, "d2h_bytes_per_call": d2h,
+               "inner_steps": r["steps"], "outer_iterations": r["outer"],
                "wall_s": r["wall"], "calls": len(runs), "wall_s_all": [round(x["wall"], 3) for x in runs],
                "phases_s": r["phases"], "host_arrays": "page-locked (qssgpu_host_alloc)",
                "pageable": {"value": dist.ws * nvox * pg["steps"] / pg["wall"], "wall_s": pg["wall"],
@@ -656,10 +695,17 @@ def main():
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)  # one GPU per rank, before CUDA starts
     dist = Dist()
     threads = os.cpu_count() or 1
+    out = ResultLine()
+    try:
+        _run(args, dist, threads, out)
+    finally:
+        out.close()
+        dist.close()
 
+
+def _run(args, dist: Dist, threads: int, out: ResultLine):
     if args.impl == "reference":
         if dist.rank != 0:
-            dist.close()
             return
         r = cpu_arm(args, args.cpu_nz, args.steps, args.warmup, threads)
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -671,19 +717,16 @@ def main():
                 "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
                                  "sample": r["sample"]},
                 "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        dist.close()
+        out.emit(line)
         return
 
     if args.adjoint_only:
         if dist.rank == 0:
-            print(json.dumps({"adjoint_mode": adjoint_arm(args)}))
-        dist.close()
+            out.emit({"adjoint_mode": adjoint_arm(args)})
         return
     if args.batch_only:
         if dist.rank == 0:
-            print(json.dumps({"batched_mode": batched_arm(args)}))
-        dist.close()
+            out.emit({"batched_mode": batched_arm(args)})
         return
     res = gpu_arm(args, dist)
     cpu = None
@@ -710,8 +753,7 @@ def main():
             line["adjoint_mode"] = adjoint_arm(args)
         if args.ladder and args.cpu:
             line["ladder_64_eno2"] = ladder_arm(threads)
-        print(json.dumps(line))
-    dist.close()
+        out.emit(line)
 
 
 if __name__ == "__main__":

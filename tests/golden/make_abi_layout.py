@@ -2,7 +2,8 @@
 the reference headers (src/geometry/qss_grid.h, src/utilities/qss_data_arrays.h,
 src/utilities/qss_options.h, FP64 build) into tests/golden/abi_layout.json.
 
-    python tests/golden/make_abi_layout.py [/path/to/reference]
+    LSMPQS_REF=/path/to/reference python tests/golden/make_abi_layout.py
+    python tests/golden/make_abi_layout.py /path/to/reference
 """
 import json
 import os
@@ -17,7 +18,9 @@ from abi_probe import probe_source  # noqa: E402
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LSMPQS_REF")
+    if not ref or not os.path.isdir(os.path.join(ref, "src")):
+        sys.exit("make_abi_layout: give the reference tree as the argument or in LSMPQS_REF")
     inc = ["-I" + os.path.join(ref, d) for d in ("config", "src/geometry", "src/utilities")]
     hdr = '#include "QSSLIB_config.h"\n#include "qss_grid.h"\n#include "qss_data_arrays.h"\n#include "qss_options.h"\n'
     with tempfile.TemporaryDirectory() as d:

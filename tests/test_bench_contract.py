@@ -1,6 +1,7 @@
 """bench.py's contract without a GPU: the reference arm (the oracle on the
-host cores) prints one JSON line with the keys the contract asks for, and
-the GB300 arm refuses to run on a machine without a CUDA device instead of
+host cores) prints one JSON line with the keys the contract asks for, as the
+last (and only) line of stdout even when C code printed before it, and the
+GB300 arm refuses to run on a machine without a CUDA device instead of
 falling back to the CPU."""
 import json
 import os
@@ -18,9 +19,9 @@ def _bench(*args, timeout=300):
 def test_reference_arm_line():
     r = _bench("--impl", "reference", "--n", "48", "--cpu-nz", "8", "--steps", "1", "--warmup", "3")
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [line for line in r.stdout.splitlines() if line.startswith("{")]
+    lines = r.stdout.strip().splitlines()
     assert len(lines) == 1
-    d = json.loads(lines[0])
+    d = json.loads(lines[-1])
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
                 "scaling", "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
         assert key in d, key
@@ -42,3 +43,21 @@ def test_gpu_arm_fails_without_a_device():
     assert r.returncode != 0
     assert "no CUDA device" in r.stderr
     assert not [line for line in r.stdout.splitlines() if line.startswith("{")]
+
+
+def test_result_line_is_last_after_buffered_c_output():
+    """The library's printf lines (the reference's progress output) sit in
+    libc's stdout buffer until exit; the result line must still be the last
+    line of stdout, and the C lines must not be lost."""
+    code = (
+        "import ctypes, sys; sys.path.insert(0, %r); import bench\n"
+        "out = bench.ResultLine()\n"
+        "libc = ctypes.CDLL(None)\n"
+        "libc.printf(b'Step 1: a = 1.250000\\n')\n"
+        "print('python progress line')\n"
+        "out.emit({'value': 1.0})\n"
+        "libc.printf(b'')\n" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout == json.dumps({"value": 1.0}) + "\n"
+    assert "Step 1: a = 1.250000" in r.stderr and "python progress line" in r.stderr
