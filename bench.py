@@ -285,14 +285,16 @@ def gpu_arm(args, dist: Dist):
                "h2d_bytes_per_call": h2d, "d2h_bytes_per_call": d2h,
                "inner_steps": r["steps"], "outer_iterations": r["outer"],
                "wall_s": r["wall"], "calls": len(runs), "wall_s_all": [round(x["wall"], 3) for x in runs],
-               "phases_s": r["phases"], "host_arrays": "page-locked (qssgpu_host_alloc)",
+               "phases_s": r["phases"], "device_phases_s": r["device_phases"],
+               "host_arrays": "page-locked (qssgpu_host_alloc)",
                "pageable": {"value": dist.ws * nvox * pg["steps"] / pg["wall"], "wall_s": pg["wall"],
                             "phases_s": pg["phases"]},
                "note": "one constCurvModel3d call with page-locked host arrays (the median of `calls` calls, "
                        "each on fresh arrays): uploads, inner steps, trapping, three reinitialisations, volume "
-                       "integrals, downloads; `pageable` is one call on ordinary (pageable) arrays; phases_s "
-                       "is the library's host-side split (device work is charged to the phase that waits "
-                       "for it)"}
+                       "integrals, downloads; `pageable` is one call on ordinary (pageable) arrays; "
+                       "device_phases_s is each phase's device time (CUDA events on the library's stream "
+                       "where the phase begins and ends; 'total' is their sum); phases_s is the host-side "
+                       "split, where device work is charged to the phase whose host code waits for it"}
 
     peaks, kind = measured_peaks()
     probe = (C.c_double * 2)()
@@ -369,9 +371,12 @@ def _e2e_call(lib, g, mask, phi, steps, dist, pinned=False):
         lib.qssgpu_call_stats(C.byref(w.p), C.byref(g), C.byref(steps_done), C.byref(outer))
         ph = (C.c_double * 8)()
         lib.qssgpu_call_times(C.byref(w.p), C.byref(g), ph)
+        dph = (C.c_double * 8)()
+        lib.qssgpu_call_device_times(C.byref(w.p), C.byref(g), dph)
         lib.qssgpu_release(C.byref(w.p))
         res = {"wall": dist.max(t1 - t0), "steps": steps_done.value, "outer": outer.value,
-                "phases": {k: round(ph[i], 3) for i, k in enumerate(PHASES) if k not in ("total", "setup")}}
+               "phases": {k: round(ph[i], 3) for i, k in enumerate(PHASES) if k not in ("total", "setup")},
+               "device_phases": {k: round(dph[i], 3) for i, k in enumerate(PHASES) if k != "setup"}}
     finally:
         # the page-locked buffers go back even when the call failed
         for ptr in buffers:

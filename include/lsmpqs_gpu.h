@@ -348,6 +348,11 @@ void qssgpu_call_stats(const QSS_DataArrays *p, const Grid *g, long long *inner_
    charged to the phase that waits for it, unless $QSSGPU_PHASE_SYNC=1 ends
    every phase with a stream synchronisation */
 void qssgpu_call_times(const QSS_DataArrays *p, const Grid *g, double *out);
+/* device time of the last top-level call on p by phase, from CUDA events
+   recorded on the volume's stream where each phase begins and ends: out[1..7]
+   as in qssgpu_call_times, out[0] their sum (out holds 8 doubles); waits for
+   the recorded events */
+void qssgpu_call_device_times(const QSS_DataArrays *p, const Grid *g, double *out);
 /* benchmark support: drain_model3d's set-up for curvature a0 with the arrays
    left in HBM, then timing of `steps` inner steps after `warmup`
    (out[0] total ms, out[1] mean ms per launch of the stage kernel with the
@@ -362,18 +367,25 @@ int qssgpu_fp64_peak(double *out);
 
 /* Allocation-free smoothed volume of {phi < 0} (no counterpart in the
    reference; same result, bit for bit, as qss3dvolumeregionphilessthanzero_).
-   For callers that must not allocate device memory while they run -- a
-   framework that owns all of HBM through its own pool, or code recording a
-   stream capture, where cudaMalloc cannot be recorded -- and that already hold
-   their data on the GPU.  d_phi (the ghost box gb = {0, nx-1, 0, ny-1, 0,
-   nz-1}) and d_volume (one double) are DEVICE pointers of the caller; ib is
-   the summed box; work is queued on `stream` (a cudaStream_t, NULL = default
+   For callers that must not allocate device memory while they run and that
+   already hold their data on the GPU: a framework that reserved all of HBM
+   up front for its own pool allocator (cudaMalloc then fails, or takes memory
+   the framework has planned for something else), or one that keeps several
+   streams busy and cannot afford the device-wide synchronisation that
+   cudaFree implies.  d_phi (the ghost box gb = {0, nx-1, 0, ny-1, 0, nz-1})
+   and d_volume (one double) are DEVICE pointers of the caller; ib is the
+   summed box; work is queued on `stream` (a cudaStream_t, NULL = default
    stream) and the result is in *d_volume when the stream reaches it.  The
    per-voxel contributions live in one fixed device array of 2^21 doubles
    (16 MiB) that every GPU loading the library holds until the process exits:
-   boxes of more than 2^21 voxels are rejected with QSSGPU_ERR_ARG.  The first
-   call on a device looks up that array's device address (make it before any
-   stream capture).  All calls share the array, which keeps the previous
+   boxes of more than 2^21 voxels (128^3) are rejected with QSSGPU_ERR_ARG.
+   Set-up: the first call on a device, with that device current, looks up the
+   array's device address (the CUDA runtime loads this part of the library,
+   and so creates the 16 MiB array, at that moment unless
+   CUDA_MODULE_LOADING=EAGER is set).  Make that first call before any stream
+   capture and before the caller's pool takes its memory.  The address is
+   kept for the life of the process: a cudaDeviceReset after the first call
+   is not supported.  All calls share the array, which keeps the previous
    call's contents (each call overwrites what it reads, nothing needs
    clearing): calls that can overlap on the GPU race.  Returns 0 or an error
    code (see qssgpu_last_error). */

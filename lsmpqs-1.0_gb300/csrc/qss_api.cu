@@ -456,6 +456,22 @@ void qssgpu_call_times(const QSS_DataArrays* p, const Grid* g, double* out) {
   }
 }
 
+// device time of the last top-level call on p by phase (CUDA events on the
+// volume's stream): out[0] the sum, then set-up, uploads, inner steps,
+// trapping, reinitialisation, reductions, downloads, as qssgpu_call_times
+void qssgpu_call_device_times(const QSS_DataArrays* p, const Grid* g, double* out) {
+  QSS_API_BEGIN
+  DevVolume& v = volume_for(p, g);
+  resolve_phase_events(v);
+  double sum = 0;
+  for (int k = 1; k < 8; k++) {
+    out[k] = v.phase_dev_s[k];
+    sum += out[k];
+  }
+  out[0] = sum;
+  QSS_API_END(return)
+}
+
 // statistics of the last top-level call on p: inner steps and outer iterations
 void qssgpu_call_stats(const QSS_DataArrays* p, const Grid* g, long long* inner_steps, long long* outer_iters) {
   QSS_API_BEGIN

@@ -1,15 +1,19 @@
 // qss_noalloc.cu -- an allocation-free variant of the smoothed volume integral.
 //
 // Some callers of this library must not allocate device memory while they
-// run: a host framework that owns every byte of HBM through its own pool and
-// forbids allocation once its memory plan is fixed, or code that records its
-// GPU work into a stream capture, where cudaMalloc is not a recordable
-// operation.  Such callers already hold their inputs and outputs in device
-// memory.  qssgpu_volume_noalloc() serves them: it reads phi from a device
-// pointer, writes the volume to a device pointer and keeps its only
-// intermediate data -- one contribution per fill-box voxel, summed in the
-// reference's loop order -- in the fixed array below, which the CUDA driver
-// creates with the library's module on every GPU that loads it and keeps
+// run: a host framework that reserved all of HBM up front for its own pool
+// allocator (a cudaMalloc then fails, or takes memory the framework planned
+// for something else), or one that keeps several streams busy and cannot
+// take the device-wide synchronisation that cudaFree implies.  Such callers
+// already hold their inputs and outputs in device memory.
+// qssgpu_volume_noalloc() serves them: it reads phi from a device pointer,
+// writes the volume to a device pointer and keeps its only intermediate data
+// -- one contribution per fill-box voxel, summed in the reference's loop
+// order -- in the fixed array below.  Under CUDA's default lazy module
+// loading the runtime loads this translation unit's module, and so creates
+// the array on a device, at the first call on that device (the
+// cudaGetSymbolAddress in scratch_on_current_device); with
+// CUDA_MODULE_LOADING=EAGER it exists from library load.  Either way it stays
 // until the process exits.  Nothing here calls cudaMalloc, cudaFree or any
 // allocating library routine.
 #include <mutex>
@@ -34,7 +38,9 @@ double* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  The array's
 // name is only a host-side stand-in; the address is looked up once per device
-// with that device current.
+// with that device current and kept for the life of the process (a
+// cudaDeviceReset after the first call would leave it stale, so none is
+// supported).
 double* scratch_on_current_device() {
   int dev = 0;
   QSS_CK(cudaGetDevice(&dev));

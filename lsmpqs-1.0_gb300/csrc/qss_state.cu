@@ -40,12 +40,30 @@ static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// at most this many events per volume and call (a phase beyond it keeps its
+// host time only)
+constexpr size_t kMaxPhaseEvents = 8192;
+
 PhaseTimer::PhaseTimer(DevVolume& vol, int phase) : v(&vol), ph(phase), t0(0) {
   if (v->phase_open >= 0 && phase != PH_TOTAL) {
     v = nullptr;  // nested: counted in the enclosing phase
     return;
   }
-  if (phase != PH_TOTAL) v->phase_open = phase;
+  if (phase != PH_TOTAL) {
+    v->phase_open = phase;
+    const size_t used = 2 * v->ev_marks.size();
+    if (v->stream && used + 2 <= kMaxPhaseEvents) {
+      while (v->ev_pool.size() < used + 2) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) break;
+        v->ev_pool.push_back(e);
+      }
+      if (v->ev_pool.size() >= used + 2 && cudaEventRecord(v->ev_pool[used], v->stream) == cudaSuccess) {
+        ev = (int)used;
+        v->ev_marks.emplace_back(phase, ev);
+      }
+    }
+  }
   t0 = now_s();
 }
 
@@ -62,6 +80,7 @@ static bool phase_sync() {
 
 PhaseTimer::~PhaseTimer() {
   if (!v) return;
+  if (ev >= 0) cudaEventRecord(v->ev_pool[ev + 1], v->stream);
   if (phase_sync()) cudaStreamSynchronize(v->stream);
   v->phase_s[ph] += now_s() - t0;
   if (ph != PH_TOTAL) v->phase_open = -1;
@@ -69,7 +88,20 @@ PhaseTimer::~PhaseTimer() {
 
 void reset_phases(DevVolume& v) {
   for (double& t : v.phase_s) t = 0;
+  for (double& t : v.phase_dev_s) t = 0;
+  v.ev_marks.clear();
   v.phase_open = -1;
+}
+
+void resolve_phase_events(DevVolume& v) {
+  for (const auto& m : v.ev_marks) {
+    float ms = 0.f;
+    cudaEvent_t b = v.ev_pool[m.second], e = v.ev_pool[m.second + 1];
+    if (cudaEventSynchronize(e) == cudaSuccess && cudaEventElapsedTime(&ms, b, e) == cudaSuccess)
+      v.phase_dev_s[m.first] += ms * 1e-3;
+  }
+  v.ev_marks.clear();
+  (void)cudaGetLastError();
 }
 
 void set_error(int code, const std::string& msg) {
@@ -182,6 +214,7 @@ static void destroy_volume(DevVolume* v) {
     if (v->dplus[d]) cudaFree(v->dplus[d]);
     if (v->dminus[d]) cudaFree(v->dminus[d]);
   }
+  for (cudaEvent_t e : v->ev_pool) cudaEventDestroy(e);
   if (v->h_ctl) cudaFreeHost(v->h_ctl);
   if (v->h_scal) cudaFreeHost(v->h_scal);
   if (v->stream) cudaStreamDestroy(v->stream);

@@ -7,6 +7,7 @@
 #include <string>
 #include <initializer_list>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/lsmpqs_gpu.h"
@@ -115,6 +116,12 @@ struct DevVolume {
   // host wall time per phase of the last top-level call (PhaseTimer)
   double phase_s[8] = {};
   int phase_open = -1;
+  // device time per phase of the last top-level call: a pair of CUDA events
+  // recorded on the volume's stream where each phase begins and ends,
+  // resolved when the times are asked for
+  double phase_dev_s[8] = {};
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> ev_marks;  // (phase, index of the begin event; the end event follows)
   HostPrefault prefault;
 };
 
@@ -154,10 +161,13 @@ struct PhaseTimer {
   DevVolume* v;
   int ph;
   double t0;
+  int ev = -1;  // index of the begin event in v->ev_pool, -1 when none was recorded
   PhaseTimer(DevVolume& vol, int phase);
   ~PhaseTimer();
 };
 void reset_phases(DevVolume& v);
+// adds the recorded phase events' durations to v.phase_dev_s (waits for them)
+void resolve_phase_events(DevVolume& v);
 
 struct CallScope {
   static thread_local int depth;

@@ -171,6 +171,7 @@ def load(path: str) -> C.CDLL:
         "qssgpu_host_alloc": (C.c_void_p, [C.c_size_t]),
         "qssgpu_host_free": (None, [C.c_void_p]),
         "qssgpu_call_times": (None, [P(QSSDataArrays), P(Grid), P(C.c_double)]),
+        "qssgpu_call_device_times": (None, [P(QSSDataArrays), P(Grid), P(C.c_double)]),
         "qssgpu_loop_sum": (C.c_int, [P(C.c_double), C.c_longlong, P(C.c_double)]),
         "qss_reinitialize_mask": (None, [P(QSSDataArrays), P(Grid), P(Options)]),
         "qssgpu_create_mask_ubc": (C.c_int, [P(C.c_ubyte), P(QSSDataArrays), P(Grid), P(Options)]),

@@ -77,7 +77,16 @@ static inline double oracle_trig_core(double x, int q)
   return (n & 2) ? -v : v;
 }
 
+#ifdef ORACLE_LIBM
+/* The reference as linked: the platform libm's sine and cosine (the Fortran
+ * intrinsics SIN/COS of qss_util3d.f:348, 467 and
+ * qss_spatial_derivatives3d.f:81, 166).  Built as liboracle_libm.so, it
+ * bounds what the portable evaluation changes in the results. */
+static inline double oracle_sin(double x) { return sin(x); }
+static inline double oracle_cos(double x) { return cos(x); }
+#else
 static inline double oracle_sin(double x) { return oracle_trig_core(x, 0); }
 static inline double oracle_cos(double x) { return oracle_trig_core(x, 1); }
+#endif
 
 #endif

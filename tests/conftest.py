@@ -14,6 +14,7 @@ for p in (PKG, os.path.join(ROOT, "tests")):
         sys.path.insert(0, p)
 
 ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle.so")
+ORACLE_LIBM_LIB = os.path.join(ORACLE_DIR, "liboracle_libm.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libqss_ref.so")
 SCRATCH = os.path.join(ROOT, ".test_tmp")
 
@@ -29,8 +30,8 @@ def pytest_configure(config):
 
 
 def _ensure_oracle():
-    if not os.path.exists(ORACLE_LIB):
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
+    if not os.path.exists(ORACLE_LIB) or not os.path.exists(ORACLE_LIBM_LIB):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so", "liboracle_libm.so"], check=True)
 
 
 @pytest.fixture(scope="session")
@@ -43,13 +44,26 @@ def oracle():
     return lib
 
 
+@pytest.fixture(scope="session")
+def oracle_libm():
+    """The oracle with the platform libm's sin/cos (the reference as linked)
+    in place of the portable evaluation both the oracle and the GPU use."""
+    import qssgpu as Q
+
+    _ensure_oracle()
+    lib = Q.load(ORACLE_LIBM_LIB)
+    lib.oracle_set_threads(1)
+    return lib
+
+
 @pytest.fixture(autouse=True)
 def _oracle_one_thread(request):
     """The reference's CFL step depends on the OpenMP thread count; other
     libraries in the process (torch) may resize the shared OpenMP pool, so
     every test that uses the oracle starts it on one thread."""
-    if "oracle" in request.fixturenames:
-        request.getfixturevalue("oracle").oracle_set_threads(1)
+    for name in ("oracle", "oracle_libm"):
+        if name in request.fixturenames:
+            request.getfixturevalue(name).oracle_set_threads(1)
     yield
 
 

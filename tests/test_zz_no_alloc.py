@@ -1,8 +1,9 @@
 """The allocation-free volume entry point, for callers that cannot allocate
-device memory while they run (a framework owning all of HBM through its own
-pool, or code recording a stream capture).  It must return, through device
-pointers, exactly what the allocating entry point returns for the same phi,
-call after call (the fixed scratch array keeps the previous call's data)."""
+device memory while they run (a framework that reserved all of HBM for its
+own pool allocator, or one that cannot take the device-wide synchronisation
+of cudaFree).  It must return, through device pointers, exactly what the
+allocating entry point and the oracle return for the same phi, call after
+call (the fixed scratch array keeps the previous call's data)."""
 import ctypes as C
 
 import numpy as np
@@ -33,6 +34,11 @@ def test_volume_noalloc_matches_allocating_entry_point(gpu, oracle):
         gpu.qss3dvolumeregionphilessthanzero_(C.byref(want), Q.dptr(phi), *Q.gb_args(g), *Q.fb_args(g),
                                               Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]), Q.dref(eps))
         Q.check(gpu)
+        # the oracle's restatement of qss3dVolumeRegionPhiLessThanZero (qss_util3d.f:288-358)
+        ref = C.c_double(-2.0)
+        oracle.qss3dvolumeregionphilessthanzero_(C.byref(ref), Q.dptr(phi), *Q.gb_args(g), *Q.fb_args(g),
+                                                 Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]), Q.dref(eps))
+        assert want.value == ref.value, (want.value, ref.value)
         d_phi = torch.from_numpy(phi).to("cuda")
         d_vol = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
