@@ -453,15 +453,17 @@ def batched_arm(args):
 
     # plain path: one volume at a time (the drain_model3d ladder without its
     # per-step files, as in the batched run)
-    plain, stats, phases_plain = [], [], []
+    plain, stats, phases_plain, walls = [], [], [], []
     t0 = time.perf_counter()
     for n, g, v, o in vols:
         w, oo = clone(v), copy_opts(o)
         one_o = (C.POINTER(Q.Options) * 1)(C.pointer(oo))
         one_p = (C.POINTER(Q.QSSDataArrays) * 1)(C.pointer(w.p))
         one_g = (C.POINTER(Q.Grid) * 1)(C.pointer(g))
+        tv = time.perf_counter()
         if lib.qssgpu_ladder_batch(1, 1, one_o, one_p, one_g, None, None, 1):
             Q.check(lib)
+        walls.append(time.perf_counter() - tv)
         s_in, s_out = C.c_longlong(0), C.c_longlong(0)
         lib.qssgpu_call_stats(C.byref(w.p), C.byref(g), C.byref(s_in), C.byref(s_out))
         stats.append(s_in.value)
@@ -494,12 +496,24 @@ def batched_arm(args):
     sum_plain = {k: round(sum(p[i] for p in phases_plain), 3) for i, k in enumerate(names)}
     sum_batch = {k: round(sum(p[i] for p in phases_batch), 3) for i, k in enumerate(names)}
     work = sum(float(n) ** 3 * st for (n, *_), st in zip(vols, stats))
+    # Roof of any batching of these volumes: the best rate one volume reached
+    # alone on the plain path (a large one, whose kernels fill the GPU) is
+    # taken as the rate the GPU sustains on this work; overlapping volumes
+    # can win back the rest of the plain path's time, no more.
+    rates = [float(n) ** 3 * st / t for (n, *_), st, t in zip(vols, stats, walls) if t > 0]
+    best = max(rates) if rates else 0.0
+    roof = {"best_single_volume_rate": best,
+            "best_single_volume_side": int(vols[rates.index(best)][0]) if rates else None,
+            "speedup_bound": t_plain / (work / best) if best > 0 else None,
+            "batched_over_best_rate": (work / t_batch) / best if best > 0 else None,
+            "note": "speedup_bound = plain wall time / (all voxel-steps at the best rate one volume reached "
+                    "alone on the plain path); batched_over_best_rate = the batch's rate over that rate"}
     return {"volumes": nv, "sides": [int(x) for x in (sides.min(), sides.max())],
             "fill_voxels": int(sum(int(x) ** 3 for x in sides)), "ladder_steps": args.batch_steps,
             "inner_steps_total": int(sum(stats)), "workers": args.batch_workers or nv,
             "plain": {"value": work / t_plain, "wall_s": t_plain},
             "batched": {"value": work / t_batch, "wall_s": t_batch},
-            "speedup": t_plain / t_batch, "per_volume_exact": bool(exact), "unit": UNIT,
+            "speedup": t_plain / t_batch, "per_volume_exact": bool(exact), "unit": UNIT, "roof": roof,
             "phase_seconds_summed_over_volumes": {"plain": sum_plain, "batched": sum_batch},
             "note": "wall clock of drain_model3d ladders with host arrays (WENO5 + TVD-RK3, tplot 0.02, "
                     "tmax 0.05, reinit and trapping included, no per-step files); plain = one volume "
@@ -689,8 +703,8 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-ckpt", type=int, default=20)
     ap.add_argument("--axis-variant", type=int, default=None,
-                    help="WENO5 axis passes: 0 registers, 1 shared memory, 2 launch shapes tuned by timing "
-                         "(default: form by size)")
+                    help="WENO5 axis passes: 0 registers, 1 shared memory, 2 launch shapes tuned by timing, "
+                         "3 tiles with one voxel per thread (default: form by size)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the roofline kernel (overrides the measured table)")
     args = ap.parse_args()
@@ -747,7 +761,7 @@ def _run(args, dist: Dist, threads: int, out: ResultLine):
                            "n": args.n, "ghost": 3, "dx": 0.04, "parallelism": f"replicas x{dist.ws}",
                            "l2": "inputs larger than L2 (each FP64 array 1.1 GB)",
                            "axis_variant": {None: "by size", 0: "registers", 1: "shared memory",
-                                            2: "tuned"}.get(args.axis_variant, args.axis_variant)},
+                                            2: "tuned", 3: "tiles"}.get(args.axis_variant, args.axis_variant)},
                 "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "roofline": res["roofline"],
                 "cpu_baseline": cpu, "clocks": res["clocks"]}
         if res["axis_tuning"]:

@@ -351,6 +351,124 @@ __global__ void __launch_bounds__(128, RING ? 5 : 4) k_weno_axis(AxisArgs a) {
   }
 }
 
+// Tile form of the axis pass: one block holds a tile of TL lines x TP voxels
+// along the pass axis, and every face, centre and eps value of the tile is
+// computed once, by one thread, into shared memory; after a barrier each
+// thread finishes one voxel (the two weight sets and the combinations).
+// Unlike the sliding-window forms no thread carries a window of faces and
+// centres in registers, so the kernel fits 64 registers per thread and eight
+// warps per scheduler stay resident to hide the latency of the integer-pipe
+// arithmetic.  The cost is the tile's halo: 21 faces and 18 centres for 16
+// voxels of a line (about 6 % more FP64 work per voxel than a long window).
+// Lanes run over the tile's lines (16) and its positions (2 per warp-row),
+// so every warp instruction of every phase is full.
+constexpr int TL = 16, TP = 16;
+constexpr int TF = TP + 5;  // faces s0-2 .. s0+TP+2
+constexpr int TC = TP + 2;  // centres s0-1 .. s0+TP
+constexpr int TE = TP + 1;  // eps+ of voxels s0-1 .. s0+TP-1
+
+template <int AX, int EMU>
+__global__ void __launch_bounds__(256, 4) k_weno_tile(AxisArgs a) {
+  if (a.ctl && !a.ctl->active) return;
+  const Box& b = a.b;
+  // faces: v, w, 3v and the five scaled copies; centres: six smoothness
+  // indicators; eps+ per voxel; all [field][position][line]
+  __shared__ double sf[8][TF][TL];
+  __shared__ double sc[6][TC][TL];
+  __shared__ double se[TE][TL];
+  const int line = threadIdx.x & (TL - 1);
+  const int slot = threadIdx.x >> 4;  // 0..15: position within a round
+  int p, q, lo, hi, plast_line;
+  if (AX == 0) {
+    p = b.jlo + blockIdx.x * TL + line;  // j
+    q = b.klo + blockIdx.y;              // k
+    lo = b.ilo;
+    hi = b.ihi;
+    plast_line = b.jhi;
+  } else {
+    p = b.ilo + blockIdx.x * TL + line;  // i
+    q = (AX == 1 ? b.klo : b.jlo) + blockIdx.y;
+    lo = (AX == 1) ? b.jlo : b.klo;
+    hi = (AX == 1) ? b.jhi : b.khi;
+    plast_line = b.ihi;
+  }
+  const bool line_ok = p <= plast_line;
+  if (!line_ok) p = plast_line;  // loads stay in the box; nothing is stored
+  const int s0 = lo + blockIdx.z * TP;
+  int64_t base, stride;
+  if (AX == 0) {
+    base = b.idx(0, p, q);
+    stride = 1;
+  } else if (AX == 1) {
+    base = b.idx(p, 0, q);
+    stride = b.nx;
+  } else {
+    base = b.idx(p, q, 0);
+    stride = (int64_t)b.nx * b.ny;
+  }
+  const double* __restrict__ phi = a.phi;
+  const int last = (AX == 0 ? b.nx : (AX == 1 ? b.ny : b.nz)) - 1;
+  auto ld = [&](int m) -> double {
+    const int mm = m > last ? last : m;
+    return __ldg(phi + base + (int64_t)mm * stride);
+  };
+
+  // faces m = s0-2+f (between voxels m-1 and m)
+  for (int f = slot; f < TF; f += 16) {
+    const int m = s0 - 2 + f;
+    const Face fc = make_face_e<EMU>(ld(m), ld(m - 1), a.inv);
+    sf[0][f][line] = fc.v;
+    sf[1][f][line] = fc.w;
+    sf[2][f][line] = fc.t3;
+    sf[3][f][line] = fc.c13;
+    sf[4][f][line] = fc.c76;
+    sf[5][f][line] = fc.c116;
+    sf[6][f][line] = fc.c16;
+    sf[7][f][line] = fc.c56;
+  }
+  __syncthreads();
+  // centres s0-1+c from faces c, c+1, c+2; eps+ of voxel s0-1+e from faces e .. e+4
+  for (int c = slot; c < TC; c += 16) {
+    Face fa{}, fb{}, fd{};
+    fa.v = sf[0][c][line];
+    fa.t3 = sf[2][c][line];
+    fb.v = sf[0][c + 1][line];
+    fd.v = sf[0][c + 2][line];
+    fd.t3 = sf[2][c + 2][line];
+    const Centre ct = make_centre<EMU, true>(fa, fb, fd);
+    sc[0][c][line] = ct.s1p;
+    sc[1][c][line] = ct.s2p;
+    sc[2][c][line] = ct.s3p;
+    sc[3][c][line] = ct.s1m;
+    sc[4][c][line] = ct.s2m;
+    sc[5][c][line] = ct.s3m;
+    if (c < TE)
+      se[c][line] = eps_of(sf[1][c + 4][line], sf[1][c + 3][line], sf[1][c + 2][line], sf[1][c + 1][line],
+                           sf[1][c][line]);
+  }
+  __syncthreads();
+  const int t = slot;
+  const int i = s0 + t;
+  if (!line_ok || i > hi) return;
+  auto F = [&](int field, int f) -> double { return sf[field][f][line]; };
+  // plus: v1..v5 = faces i+3, i+2, i+1, i, i-1 (tile faces t+5 .. t+1)
+  const double pp1_ = (F(3, t + 5) - F(4, t + 4)) + F(5, t + 3);
+  const double pp2_ = (-F(6, t + 4) + F(7, t + 3)) + F(3, t + 2);
+  const double pp3_ = (F(3, t + 3) + F(7, t + 2)) - F(6, t + 1);
+  const double plus =
+      weno_weights<EMU, true>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line], sc[2][t + 1][line],
+                              se[t + 1][line]);
+  // minus: v1..v5 = faces i-2, i-1, i, i+1, i+2 (tile faces t .. t+4)
+  const double pm1_ = (F(3, t) - F(4, t + 1)) + F(5, t + 2);
+  const double pm2_ = (-F(6, t + 1) + F(7, t + 2)) + F(3, t + 3);
+  const double pm3_ = (F(3, t + 2) + F(7, t + 3)) - F(6, t + 4);
+  const double minus =
+      weno_weights<EMU, true>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line], se[t][line]);
+  const int64_t o = base + (int64_t)i * stride;
+  a.dplus[o] = plus;
+  a.dminus[o] = minus;
+}
+
 struct CombineArgs {
   Box b;
   Fac fac;
@@ -542,6 +660,13 @@ int default_seg_len(int var, int64_t lines, int along) {
 template <int EMU>
 void launch_axis(cudaStream_t s, int ax, int var, AxisArgs a, int lanes, int other, int along, int len) {
   a.seg_len = len;
+  if (var == 3 && EMU != 0) {
+    const dim3 gt((lanes + TL - 1) / TL, other, (along + TP - 1) / TP);
+    if (ax == 0) k_weno_tile<0, EMU><<<gt, 256, 0, s>>>(a);
+    else if (ax == 1) k_weno_tile<1, EMU><<<gt, 256, 0, s>>>(a);
+    else k_weno_tile<2, EMU><<<gt, 256, 0, s>>>(a);
+    return;
+  }
   dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
   if (EMU == 0 || var == 0) {
     if (ax == 0) k_weno_axis<0, EMU, false><<<g, 128, 0, s>>>(a);
@@ -622,7 +747,8 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     // the shared-memory form is the faster one from ~12 M fill voxels on
     // (measured on GB300, register / shared-memory form, M voxel-steps/s:
     // 128^3 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
-    int var = mode == 0 || mode == 1 ? mode : ((int64_t)lanes * other * along >= kRingVoxels ? 1 : 0);
+    int var = mode == 0 || mode == 1 || mode == 3 ? mode
+                                                  : ((int64_t)lanes * other * along >= kRingVoxels ? 1 : 0);
     int len = EMU == 0 ? SEG : default_seg_len(var, (int64_t)lanes * other, along);
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
     if (mode == 2 && EMU != 0) {

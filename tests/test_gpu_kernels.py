@@ -74,15 +74,16 @@ def test_rhs_slab_and_tiny_speed(gpu, oracle, name, var):
 
 
 @pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 0), (1, 1, 1), (1, 2, 0),
-                                               (1, 2, 1), (1, 1, 2), (1, 2, 2)])
+                                               (1, 2, 1), (1, 1, 2), (1, 2, 2), (1, 1, 3), (1, 2, 3)])
 @pytest.mark.parametrize("small", [0.0, 0.2])
 def test_weno5_split_and_fused(gpu, oracle, split, emu, variant, small):
     """The WENO5 stage runs as one fused kernel (split 0) or as one kernel per
     axis with shared sub-expressions + a combine kernel (split 1), with 0, 1
     or 2 levels of FP64 arithmetic on the integer pipes and the axis passes'
-    window in registers (variant 0), partly in shared memory (1) or the
-    launch shape tuned by timing (2); all equal the oracle bit for bit, on
-    the whole fill box and on a z-slab."""
+    window in registers (variant 0), partly in shared memory (1), the
+    launch shape tuned by timing (2) or tiles of one voxel per thread with
+    faces and centres in shared memory (3); all equal the oracle bit for bit,
+    on the whole fill box and on a z-slab."""
     g, _ = pack_case(oracle, N)
     phi, vel, b, vx, vy, vz = _fields(g, 5, small)
     prev = gpu.qssgpu_set_weno_split(split)

@@ -150,7 +150,7 @@ def _device_ladder_files(gpu, g, v0, o, imbibe_a, imbibe_min):
         for f in os.listdir(d):
             if "data_step" in f:
                 with gzip.open(os.path.join(d, f), "rb") as fh:
-                    files[f] = fh.read()
+                    files[f[:-3] if f.endswith(".gz") else f] = fh.read()
         return files
 
     files = in_tmpdir(go)

@@ -111,7 +111,7 @@ def test_const_curv_model(gpu, oracle, theta, space, time):
 
 
 @pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 1), (1, 2, 0), (1, 2, 1),
-                                               (1, 2, 2)])
+                                               (1, 2, 2), (1, 2, 3)])
 def test_const_curv_model_weno_modes(gpu, oracle, split, emu, variant):
     """WENO5 + TVD-RK3 with variable coefficients through the fused stage
     kernel and through the axis passes (both forms) + combine: all equal the
