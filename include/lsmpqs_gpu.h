@@ -231,7 +231,9 @@ int qssgpu_set_emu_level(int level);
    launch (the second form from ~12 M fill voxels), 2 tuned: the first pass
    over each line shape times every distinct (form, segment length) and the
    fastest is kept for that shape (one stream synchronisation per new shape
-   and axis); identical results; returns the previous setting.  No
+   and axis), 3 and 4 tiles of 16 lines x 16 (3) or 32 (4) voxels, one voxel
+   per thread, every face and centre of a tile computed once into shared
+   memory; identical results; returns the previous setting.  No
    reference counterpart: the reference's getrhs3d5th_ (3d.f:1962-2246) is a
    loop over voxels with nothing to tune. */
 int qssgpu_set_axis_variant(int variant);

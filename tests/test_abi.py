@@ -118,14 +118,15 @@ def test_host_side_argument_checks(lib):
 
 
 def test_axis_variant_settings(lib):
-    """The axis-pass form setting takes -1 (by size), 0, 1, 2 (tuned) and 3
-    (tiles), clamps larger values to 3, returns the previous setting, and the
-    tuned shape table starts empty and can be cleared."""
+    """The axis-pass form setting takes -1 (by size), 0, 1, 2 (tuned), 3 and 4
+    (tiles of 16 and 32 voxels a line), clamps larger values to 4, returns the
+    previous setting, and the tuned shape table starts empty and can be
+    cleared."""
     L = Q.load(Q.GPU_LIB)
     prev = L.qssgpu_set_axis_variant(2)
     try:
         assert L.qssgpu_set_axis_variant(7) == 2
-        assert L.qssgpu_set_axis_variant(0) == 3
+        assert L.qssgpu_set_axis_variant(0) == 6
         assert L.qssgpu_set_axis_variant(-5) == 0
     finally:
         L.qssgpu_set_axis_variant(prev)

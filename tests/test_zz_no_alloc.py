@@ -64,3 +64,36 @@ def test_volume_noalloc_rejects_boxes_beyond_its_scratch(gpu):
     msg = gpu.qssgpu_error_string().decode()
     gpu.qssgpu_clear_error()
     assert "scratch" in msg
+
+
+def test_volume_noalloc_on_a_caller_stream_takes_no_device_memory(gpu, oracle):
+    """On a stream of the caller's, after a first call that did the set-up,
+    further calls leave the device's free memory unchanged and still return
+    the allocating entry point's volume."""
+    torch = pytest.importorskip("torch")
+    noalloc = _bind(gpu)
+    g, v = pack_case(oracle, 32, seed=9)
+    phi = v["phi"]
+    eps = 1.5 * g.dx[0]
+    want = C.c_double(-1.0)
+    gpu.qss3dvolumeregionphilessthanzero_(C.byref(want), Q.dptr(phi), *Q.gb_args(g), *Q.fb_args(g),
+                                          Q.dref(g.dx[0]), Q.dref(g.dx[1]), Q.dref(g.dx[2]), Q.dref(eps))
+    Q.check(gpu)
+    gb = (C.c_int * 6)(g.ilo_gb, g.ihi_gb, g.jlo_gb, g.jhi_gb, g.klo_gb, g.khi_gb)
+    ib = (C.c_int * 6)(g.ilo_fb, g.ihi_fb, g.jlo_fb, g.jhi_fb, g.klo_fb, g.khi_fb)
+    d_phi = torch.from_numpy(phi).to("cuda")
+    d_vol = torch.zeros(2, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    assert noalloc(d_phi.data_ptr(), gb, ib, g.dx[0], g.dx[1], g.dx[2], eps, d_vol.data_ptr(),
+                   C.c_void_p(side.cuda_stream)) == 0
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert noalloc(d_phi.data_ptr(), gb, ib, g.dx[0], g.dx[1], g.dx[2], eps, d_vol[1:].data_ptr(),
+                       C.c_void_p(side.cuda_stream)) == 0
+    side.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    Q.check(gpu)
+    assert free_after == free_before
+    assert d_vol[0].item() == want.value and d_vol[1].item() == want.value
