@@ -118,11 +118,9 @@ struct Centre {
 // three indicators of the plus side (S1+(c-2), S2+(c-1), S3+(c)) and of the
 // minus side (S1-(c+1), S2-(c), S3-(c-1)), each as first term + second term
 // in the reference's order of operations
-template <int EMU, bool SQ, bool ADDS = false>
+template <int EMU, bool SQ>
 __device__ __forceinline__ Centre make_centre(const Face& a, const Face& b, const Face& d) {
   using Q = Ar<EMU>;
-  // the six indicator sums on the integer pipes when ADDS
-  auto add = [](double x, double y) { return ADDS ? qss_emu::add(x, y) : x + y; };
   // squares (and the 13/12 products) on the integer pipes when SQ
   auto sq = [](double t) { return SQ ? Q::mul2(t, t) : t * t; };
   auto k13 = [](double x) { return SQ ? Q::mul2(k1312, x) : k1312 * x; };
@@ -143,12 +141,12 @@ __device__ __forceinline__ Centre make_centre(const Face& a, const Face& b, cons
   t = d.v - a.v;
   const double E = Q::s2(sq(t), -2);
   Centre c;
-  c.s1p = add(A, Cp);
-  c.s2p = add(A, E);
-  c.s3p = add(A, Dp);
-  c.s1m = add(B, Cm);
-  c.s2m = add(B, E);
-  c.s3m = add(B, Dm);
+  c.s1p = A + Cp;
+  c.s2p = A + E;
+  c.s3p = A + Dp;
+  c.s1m = B + Cm;
+  c.s2m = B + E;
+  c.s3m = B + Dm;
   return c;
 }
 
@@ -160,21 +158,19 @@ __device__ __forceinline__ double eps_of(double w1, double w2, double w3, double
 
 // weights and combination of one side (3d.f:1996-2005) given the candidate
 // stencils and smoothness indicators
-template <int EMU, bool SQ, bool ADDS = false>
+template <int EMU, bool SQ>
 __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, double S1, double S2, double S3,
                                                double eps) {
   using Q = Ar<EMU>;
   auto sq = [](double t) { return SQ ? Q::mul2(t, t) : t * t; };
-  // S + eps and the weights' sum on the integer pipes when ADDS
-  auto add = [](double x, double y) { return ADDS ? qss_emu::add(x, y) : x + y; };
   double t, a1, a2, a3;
-  t = add(S1, eps);
+  t = S1 + eps;
   a1 = Q::div(0.1, sq(t));
-  t = add(S2, eps);
+  t = S2 + eps;
   a2 = Q::div(0.6, sq(t));
-  t = add(S3, eps);
+  t = S3 + eps;
   a3 = Q::div(0.3, sq(t));
-  const double inv_sum_a = Q::div(1.0, add(add(a1, a2), a3));
+  const double inv_sum_a = Q::div(1.0, a1 + a2 + a3);
   a1 = Q::mul2(a1, inv_sum_a);
   a2 = Q::mul2(a2, inv_sum_a);
   a3 = Q::mul2(a3, inv_sum_a);
@@ -360,45 +356,41 @@ __global__ void __launch_bounds__(128, RING ? 5 : 4) k_weno_axis(AxisArgs a) {
 // computed once, by one thread, into shared memory; after a barrier each
 // thread finishes one voxel (the two weight sets and the combinations).
 // Unlike the sliding-window forms no thread carries a window of faces and
-// centres in registers, so the kernel fits 64 registers per thread and eight
-// warps per scheduler stay resident to hide the latency of the integer-pipe
-// arithmetic.  The cost is the tile's halo: 21 faces and 19 centres for 16
-// voxels of a line (about 7 % more FP64 work per voxel than a long window).
-// Lanes run over the tile's lines (16) and its positions (2 per warp-row),
-// so every warp instruction of every phase is full.
-constexpr int TL = 16;
+// centres in registers, so the kernel fits 48 registers per thread and five
+// blocks (ten warps per scheduler) stay resident to hide the latency of the
+// integer-pipe arithmetic and of the tile's barriers.  The cost is the tile's
+// halo: 21 faces and 19 centres for 16 voxels of a line (about 7 % more FP64
+// work per voxel than a long window).  Lanes run over the tile's lines (16)
+// and its positions (2 per warp row), so every warp instruction of every
+// phase is full.  Measured on GB300 (whole WENO5 stage, M voxel-steps/s,
+// by-size default of the window forms -> tiles): 64^3 188 -> 338, 128^3
+// 418 -> 476, 192^3 411 -> 501, 256^3 474 -> 509, 384^3 485 -> 514, 512^3
+// 497 -> 516; the FP64 pipe runs 76 % busy at 192^3 (ncu, 4 blocks per SM)
+// against 57 % for the window form.
+constexpr int TL = 16, TP = 16;
+constexpr int TF = TP + 5;  // faces s0-2 .. s0+TP+2
+constexpr int TC = TP + 3;  // centres s0-1 .. s0+TP+1
+constexpr int TE = TP + 1;  // eps+ of voxels s0-1 .. s0+TP-1
+constexpr int TNT = TL * TP;
+constexpr size_t TILE_BYTES = sizeof(double) * (8 * TF + 6 * TC + TE) * TL;
 
-// TP voxels per line and tile (16 or 32), TL * TP threads
-template <int TP>
-struct TileShape {
-  static constexpr int NT = TL * TP;
-  static constexpr int TF = TP + 5;  // faces s0-2 .. s0+TP+2
-  static constexpr int TC = TP + 3;  // centres s0-1 .. s0+TP+1
-  static constexpr int TE = TP + 1;  // eps+ of voxels s0-1 .. s0+TP-1
-  static constexpr int MIN_BLOCKS = TP == 16 ? 4 : 2;
-  static constexpr size_t BYTES = sizeof(double) * (8 * TF + 6 * TC + TE) * TL;
-};
-
-// opts a tile kernel in to its dynamic shared memory above 48 KB (once per
-// process and kernel)
+// the tile kernels ask for all of the unified L1 / shared memory as shared
+// memory, so that five blocks of TILE_BYTES fit on an SM (once per process
+// and kernel)
 template <typename K>
-void tile_smem_attr(K kernel, size_t bytes, bool& done) {
+void tile_smem_attr(K kernel, bool& done) {
   if (done) return;
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  // all of the unified L1 / shared memory as shared memory, so that the
-  // occupancy the launch bounds ask for fits
   cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   done = true;
 }
 
-template <int AX, int EMU, int TP, bool ADDS, int MINB>
-__global__ void __launch_bounds__(TileShape<TP>::NT, MINB) k_weno_tile(AxisArgs a) {
+template <int AX, int EMU>
+__global__ void __launch_bounds__(TNT, 5) k_weno_tile(AxisArgs a) {
   if (a.ctl && !a.ctl->active) return;
-  constexpr int TF = TileShape<TP>::TF, TC = TileShape<TP>::TC, TE = TileShape<TP>::TE;
   const Box& b = a.b;
   // faces: v, w, 3v and the five scaled copies; centres: six smoothness
   // indicators; eps+ per voxel; all [field][position][line], in dynamic
-  // shared memory (TileShape<TP>::BYTES)
+  // shared memory (TILE_BYTES)
   extern __shared__ double tile_smem[];
   auto sf = reinterpret_cast<double(*)[TF][TL]>(tile_smem);
   auto sc = reinterpret_cast<double(*)[TC][TL]>(tile_smem + 8 * TF * TL);
@@ -462,7 +454,7 @@ __global__ void __launch_bounds__(TileShape<TP>::NT, MINB) k_weno_tile(AxisArgs 
     fb.v = sf[0][c + 1][line];
     fd.v = sf[0][c + 2][line];
     fd.t3 = sf[2][c + 2][line];
-    const Centre ct = make_centre<EMU, true, ADDS>(fa, fb, fd);
+    const Centre ct = make_centre<EMU, true>(fa, fb, fd);
     sc[0][c][line] = ct.s1p;
     sc[1][c][line] = ct.s2p;
     sc[2][c][line] = ct.s3p;
@@ -483,15 +475,15 @@ __global__ void __launch_bounds__(TileShape<TP>::NT, MINB) k_weno_tile(AxisArgs 
   const double pp2_ = (-F(6, t + 4) + F(7, t + 3)) + F(3, t + 2);
   const double pp3_ = (F(3, t + 3) + F(7, t + 2)) - F(6, t + 1);
   const double plus =
-      weno_weights<EMU, true, ADDS>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line],
-                                    sc[2][t + 1][line], se[t + 1][line]);
+      weno_weights<EMU, true>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line], sc[2][t + 1][line],
+                              se[t + 1][line]);
   // minus: v1..v5 = faces i-2, i-1, i, i+1, i+2 (tile faces t .. t+4)
   const double pm1_ = (F(3, t) - F(4, t + 1)) + F(5, t + 2);
   const double pm2_ = (-F(6, t + 1) + F(7, t + 2)) + F(3, t + 3);
   const double pm3_ = (F(3, t + 2) + F(7, t + 3)) - F(6, t + 4);
   const double minus =
-      weno_weights<EMU, true, ADDS>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line],
-                                    se[t][line]);
+      weno_weights<EMU, true>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line],
+                              se[t][line]);
   const int64_t o = base + (int64_t)i * stride;
   a.dplus[o] = plus;
   a.dminus[o] = minus;
@@ -685,33 +677,27 @@ int default_seg_len(int var, int64_t lines, int along) {
   return var ? seg_len_for(lines, along, 16, along / 64) : seg_len_for(lines, along, 8, (along + SEG - 1) / SEG);
 }
 
-template <int EMU, int TP, bool ADDS, int MINB = TileShape<TP>::MIN_BLOCKS>
+template <int EMU>
 void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
-  constexpr size_t sm = TileShape<TP>::BYTES;
   const dim3 gt((lanes + TL - 1) / TL, other, (along + TP - 1) / TP);
   static bool done[3] = {false, false, false};
   if (ax == 0) {
-    tile_smem_attr(k_weno_tile<0, EMU, TP, ADDS, MINB>, sm, done[0]);
-    k_weno_tile<0, EMU, TP, ADDS, MINB><<<gt, TL * TP, sm, s>>>(a);
+    tile_smem_attr(k_weno_tile<0, EMU>, done[0]);
+    k_weno_tile<0, EMU><<<gt, TNT, TILE_BYTES, s>>>(a);
   } else if (ax == 1) {
-    tile_smem_attr(k_weno_tile<1, EMU, TP, ADDS, MINB>, sm, done[1]);
-    k_weno_tile<1, EMU, TP, ADDS, MINB><<<gt, TL * TP, sm, s>>>(a);
+    tile_smem_attr(k_weno_tile<1, EMU>, done[1]);
+    k_weno_tile<1, EMU><<<gt, TNT, TILE_BYTES, s>>>(a);
   } else {
-    tile_smem_attr(k_weno_tile<2, EMU, TP, ADDS, MINB>, sm, done[2]);
-    k_weno_tile<2, EMU, TP, ADDS, MINB><<<gt, TL * TP, sm, s>>>(a);
+    tile_smem_attr(k_weno_tile<2, EMU>, done[2]);
+    k_weno_tile<2, EMU><<<gt, TNT, TILE_BYTES, s>>>(a);
   }
 }
 
 template <int EMU>
 void launch_axis(cudaStream_t s, int ax, int var, AxisArgs a, int lanes, int other, int along, int len) {
   a.seg_len = len;
-  if (var >= 3 && EMU != 0) {
-    // 3: tiles of 16 voxels a line, 4: 32 voxels, 5: 16 voxels with the
-    // indicator and weight sums on the integer pipes
-    if (var == 4) launch_tile<EMU, 32, false>(s, ax, a, lanes, other, along);
-    else if (var == 5) launch_tile<EMU, 16, true>(s, ax, a, lanes, other, along);
-    else if (var == 6) launch_tile<EMU, 16, false, 5>(s, ax, a, lanes, other, along);
-    else launch_tile<EMU, 16, false>(s, ax, a, lanes, other, along);
+  if (var == 3 && EMU != 0) {
+    launch_tile<EMU>(s, ax, a, lanes, other, along);
     return;
   }
   dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
@@ -749,6 +735,7 @@ bool tune_axis(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, 
     for (const auto& d : cand) seen = seen || d == c;
     if (!seen) cand.push_back(c);
   };
+  add(3, TP);  // the tile form (its segment is the tile)
   for (int v = 0; v < 2; v++) {
     add(v, default_seg_len(v, lines, along));
     for (int64_t waves : {2, 4, 8, 16, 32}) add(v, seg_len_for(lines, along, waves, (along + SEG - 1) / SEG));
@@ -791,11 +778,13 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     const int along = ax == 0 ? b.fbx() : (ax == 1 ? b.fby() : b.fbz());
     const int lanes = ax == 0 ? b.fby() : b.fbx();
     const int other = ax == 2 ? b.fby() : b.fbz();
-    // the shared-memory form is the faster one from ~12 M fill voxels on
-    // (measured on GB300, register / shared-memory form, M voxel-steps/s:
-    // 128^3 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
-    int var = mode == 0 || mode == 1 || mode >= 3 ? mode
-                                                  : ((int64_t)lanes * other * along >= kRingVoxels ? 1 : 0);
+    // by default the tile form, the fastest at every size measured on GB300
+    // (64^3 .. 512^3, see k_weno_tile); of the two window forms, which are
+    // kept selectable, the shared-memory one is the faster from ~12 M fill
+    // voxels on (register / shared-memory form, M voxel-steps/s: 128^3
+    // 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
+    int var = mode == 0 || mode == 1 || mode == 3 ? mode : 3;
+    if (mode == 2) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
     int len = EMU == 0 ? SEG : default_seg_len(var, (int64_t)lanes * other, along);
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
     if (mode == 2 && EMU != 0) {
@@ -930,7 +919,7 @@ int qssgpu_axis_tuning_load(const char* path) {
     char tail;
     ok = sscanf(c, "%d %d %d %d %d %d %d %c", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &tail) == 7 &&
          v[0] >= 1 && v[0] <= 2 && v[1] >= 0 && v[1] <= 2 && v[2] > 0 && v[3] > 0 && v[4] > 0 &&
-         (v[5] == 0 || v[5] == 1) && v[6] >= 1 && v[6] <= v[4];
+         (v[5] == 0 || v[5] == 1 || v[5] == 3) && v[6] >= 1 && (v[5] == 3 ? v[6] == qss::TP : v[6] <= v[4]);
     if (ok) rows.push_back({qss::TuneKey{v[0], v[1], v[2], v[3], v[4]}, std::array<int, 2>{v[5], v[6]}});
   }
   fclose(fp);

@@ -118,15 +118,15 @@ def test_host_side_argument_checks(lib):
 
 
 def test_axis_variant_settings(lib):
-    """The axis-pass form setting takes -1 (by size), 0, 1, 2 (tuned), 3 and 4
-    (tiles of 16 and 32 voxels a line), clamps larger values to 4, returns the
+    """The axis-pass form setting takes -1 (default: tiles), 0, 1 (window
+    forms), 2 (tuned) and 3 (tiles), clamps larger values to 3, returns the
     previous setting, and the tuned shape table starts empty and can be
     cleared."""
     L = Q.load(Q.GPU_LIB)
     prev = L.qssgpu_set_axis_variant(2)
     try:
         assert L.qssgpu_set_axis_variant(7) == 2
-        assert L.qssgpu_set_axis_variant(0) == 6
+        assert L.qssgpu_set_axis_variant(0) == 3
         assert L.qssgpu_set_axis_variant(-5) == 0
     finally:
         L.qssgpu_set_axis_variant(prev)
@@ -138,17 +138,18 @@ def test_axis_tuning_file_round_trip(lib, tmp_path):
     """Tuned launch shapes saved to a file and loaded back (no GPU needed):
     valid rows are added, a shape already in the table keeps its pick, and a
     file with any invalid row (a segment length of 0 or longer than the line,
-    an unknown form, a bad level or axis, a short row) adds nothing."""
+    an unknown form, a tile form whose segment is not its 16 voxels, a bad
+    level or axis, a short row) adds nothing."""
     L = Q.load(Q.GPU_LIB)
     L.qssgpu_axis_tuning_reset()
     good = tmp_path / "shapes"
     good.write_text("# level axis lanes lines_per_lane line form seg_len\n"
-                    "2 0 512 512 512 1 128\n2 1 512 512 512 1 128\n\n  2 2 512 512 512 0 16\n")
+                    "2 0 512 512 512 1 128\n2 1 512 512 512 3 16\n\n  2 2 512 512 512 0 16\n")
     assert L.qssgpu_axis_tuning_load(str(good).encode()) == 3
     rows = (C.c_int * 21)()
     assert L.qssgpu_axis_tuning(rows, 7) == 3
     got = sorted(tuple(rows[7 * i:7 * i + 7]) for i in range(3))
-    assert got == [(2, 0, 512, 512, 512, 1, 128), (2, 1, 512, 512, 512, 1, 128), (2, 2, 512, 512, 512, 0, 16)]
+    assert got == [(2, 0, 512, 512, 512, 1, 128), (2, 1, 512, 512, 512, 3, 16), (2, 2, 512, 512, 512, 0, 16)]
     # the first pick of a shape stays
     other = tmp_path / "other"
     other.write_text("2 0 512 512 512 0 64\n1 0 40 40 40 0 20\n")
@@ -158,7 +159,8 @@ def test_axis_tuning_file_round_trip(lib, tmp_path):
     assert L.qssgpu_axis_tuning_save(str(back).encode()) == 4
     assert "2 0 512 512 512 1 128" in back.read_text()
     assert "2 0 512 512 512 0 64" not in back.read_text()
-    for bad in ("2 0 512 512 512 1 0", "2 0 512 512 512 1 513", "2 0 512 512 512 2 64", "3 0 8 8 8 0 8",
+    for bad in ("2 0 512 512 512 1 0", "2 0 512 512 512 1 513", "2 0 512 512 512 2 64", "2 0 512 512 512 3 17",
+                "3 0 8 8 8 0 8",
                 "2 3 8 8 8 0 8", "2 0 8 8 8 0", "2 0 8 8 8 0 8 9", "2 0 -8 8 8 0 8"):
         f = tmp_path / "bad"
         f.write_text("2 1 64 64 64 0 16\n" + bad + "\n")
