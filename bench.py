@@ -209,16 +209,28 @@ FLOP_PER_VOXEL = {0: 3 * (16 + 2 * 75) + 10 + 5 + 72 + 2 + 5,
                   1: 9 + 35 + 2 + 2 * 26, 2: 9 + 35 + 2 + 2 * 26, 3: 9 + 35 + 2 + 2 * 26,
                   4: 10 + 5 + 72 + 2 + 5}
 KERNEL_NAME = {0: "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
-               1: "k_weno_axis<0> (WENO5 x-pass, shared sub-expressions)",
-               2: "k_weno_axis<1> (WENO5 y-pass, shared sub-expressions)",
-               3: "k_weno_axis<2> (WENO5 z-pass, shared sub-expressions)",
+               1: "k_weno_tile<0> (WENO5 x-pass, 16 x 16 tiles, shared sub-expressions)",
+               2: "k_weno_tile<1> (WENO5 y-pass, 16 x 16 tiles, shared sub-expressions)",
+               3: "k_weno_tile<2> (WENO5 z-pass, 16 x 16 tiles, shared sub-expressions)",
                4: "k_weno_combine (Godunov + advection + curvature + TVD-RK)"}
+# the window forms (--axis-variant 0/1/2) run k_weno_axis<axis> instead
+WINDOW_NAME = {1: "k_weno_axis<0> (WENO5 x-pass, sliding window)",
+               2: "k_weno_axis<1> (WENO5 y-pass, sliding window)",
+               3: "k_weno_axis<2> (WENO5 z-pass, sliding window)"}
+# FP64-pipe instructions (DADD + DMUL) per fill-box voxel of one tile-form axis
+# pass, ncu at 192^3 (smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum
+# over 7.08 M voxels: 50.9 + 11.1); the rest of the 98 algorithmic operations
+# (divisions, squares, scalings, maxima, scaled copies) run on the integer pipes
+FP64_INSTR_PER_VOXEL_TILE = 62.0
 N_KINDS = 5
 # DRAM bytes per fill-box voxel of one launch of each stage kernel, measured at
 # 512^3 with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass):
 # x pass 7.74 GB, y pass 3.40 GB, z pass 3.37 GB, combine 14.22 GB for 134.2 M
 # voxels; the fused kernel was not captured
 TRAFFIC_BYTES_PER_VOXEL = {1: 57.7, 2: 25.3, 3: 25.1, 4: 105.9}
+# the same for the tile form of the axis passes (the default), measured at
+# 192^3 and scaled per voxel
+TRAFFIC_BYTES_PER_VOXEL_TILE = {}
 # algorithmic HBM bytes per voxel-step (each array touched once per stage):
 # stage 1 phi + 5 coefficients -> phi1, stage 2 phi1 + phi + 5 coeff -> phi2,
 # stage 3 phi2 + phi + 5 coeff + 3 masks -> phi1, phi
@@ -253,7 +265,12 @@ def gpu_arm(args, dist: Dist):
     value = dist.ws * nvox * args.steps / (ms / 1e3)
     top = int(out[4])
     top_ms = out[1]
-    kinds = {KERNEL_NAME[k].split(" ")[0]: {"ms_total": round(out[5 + k], 3),
+    window = args.axis_variant in (0, 1, 2)
+
+    def kname(k):
+        return (WINDOW_NAME if window and k in WINDOW_NAME else KERNEL_NAME)[k]
+
+    kinds = {kname(k).split(" ")[0]: {"ms_total": round(out[5 + k], 3),
                                             "launches": int(out[5 + N_KINDS + k]),
                                             "share_of_step": round(out[5 + k] / ms, 4) if ms else None}
              for k in range(N_KINDS) if out[5 + N_KINDS + k] > 0}
@@ -298,24 +315,49 @@ def gpu_arm(args, dist: Dist):
 
     peaks, kind = measured_peaks()
     probe = (C.c_double * 2)()
-    fp64_peak, peak_src = args.fp64_peak, "nominal GB300 FP64 (1.25 TFLOP/s)"
+    # The kernels are built without FMA contraction (bit parity), so every
+    # FP64-pipe instruction retires one operation: the ceiling of the FP64
+    # pipe for them is its non-FMA issue rate, measured by the DADD probe.
+    dfma_tflops, fp64_peak = args.fp64_peak, args.fp64_peak / 2
+    peak_src = "nominal GB300 FP64 without FMA (half of 1.25 TFLOP/s)"
     if not lib.qssgpu_fp64_peak(probe):
-        fp64_peak = round(probe[0], 4)
-        peak_src = (f"measured by the repo's DFMA probe (8 chains/thread); DADD rate {probe[1]:.3f} TFLOP/s; "
-                    "no FP64 figure in MEASURED_PEAKS.json")
+        dfma_tflops, fp64_peak = round(probe[0], 4), round(probe[1], 4)
+        peak_src = ("measured non-FMA FP64 issue rate (the repo's DADD probe, 8 chains/thread): the FP64 pipe's "
+                    "ceiling for kernels built without FMA contraction; no FP64 figure in MEASURED_PEAKS.json")
     flop_launch = FLOP_PER_VOXEL[top] * nvox
     achieved_tf = flop_launch / (top_ms / 1e3) / 1e12 if top_ms > 0 else 0.0
+    tile = top in (1, 2, 3) and not window
+    if tile or (top == 4 and not window):
+        traffic_table = dict(TRAFFIC_BYTES_PER_VOXEL_TILE)
+        traffic_unit = "bytes per launch (ncu at 192^3, scaled per voxel to this size)"
+    else:
+        traffic_table = TRAFFIC_BYTES_PER_VOXEL
+        traffic_unit = "bytes per launch (ncu at 512^3, scaled per voxel to this size)"
+    fp64_pipe = None
+    if tile and top_ms > 0:
+        instr = FP64_INSTR_PER_VOXEL_TILE * nvox / (top_ms / 1e3) / 1e12
+        fp64_pipe = {"instructions_per_voxel": FP64_INSTR_PER_VOXEL_TILE, "achieved": round(instr, 4),
+                     "peak": fp64_peak, "unit": "T instructions/s", "frac": round(instr / fp64_peak, 4),
+                     "ncu_busy_pct_192": 75.7,
+                     "note": "FP64-pipe instructions (DADD + DMUL, ncu count per voxel) over the launch time, "
+                             "against the non-FMA issue rate; ncu_busy_pct_192 is sm__inst_executed_pipe_fp64 "
+                             "(pct of peak) of the same kernel at 192^3"}
     # HBM: the step's algorithmic bytes over the time of all its stage kernels
     stage_total_ms = out[3] / args.steps
     achieved_gbs = BYTES_PER_VOXEL_STEP * nvox / (stage_total_ms / 1e3) / 1e9 if stage_total_ms > 0 else 0.0
     roofline = {"bound": "fp64", "achieved": round(achieved_tf, 4), "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": round(achieved_tf / fp64_peak, 4) if fp64_peak else None,
                 "traffic": args.traffic if args.traffic is not None else (
-                    round(TRAFFIC_BYTES_PER_VOXEL[top] * nvox) if top in TRAFFIC_BYTES_PER_VOXEL else None),
-                "traffic_unit": "bytes per launch (ncu at 512^3, scaled per voxel to this size)",
-                "kernel": KERNEL_NAME[top], "flop_per_voxel": FLOP_PER_VOXEL[top],
+                    round(traffic_table[top] * nvox) if top in traffic_table else None),
+                "traffic_unit": traffic_unit,
+                "kernel": kname(top), "flop_per_voxel": FLOP_PER_VOXEL[top],
                 "launch_ms": round(top_ms, 4), "kernels": kinds,
-                "peak_source": peak_src,
+                "peak_source": peak_src, "dfma_peak_tflops": dfma_tflops,
+                "note": "achieved = the kernel's algorithmic FP64 operations per launch over its mean launch time "
+                        "(CUDA events); about a third of them (divisions, squares, power-of-two scalings, maxima, "
+                        "scaled copies) run bit-exactly on the integer pipes, so frac against the FP64 pipe's "
+                        "non-FMA ceiling can exceed 1; fp64_pipe is the pipe's own utilisation",
+                "fp64_pipe": fp64_pipe,
                 "hbm": {"achieved": round(achieved_gbs, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                         "frac": round(achieved_gbs / peaks["hbm_gbs"], 4), "peak_kind": kind}}
     tuned = []
@@ -704,7 +746,7 @@ def main():
     ap.add_argument("--adj-ckpt", type=int, default=20)
     ap.add_argument("--axis-variant", type=int, default=None,
                     help="WENO5 axis passes: 0 registers, 1 shared memory, 2 launch shapes tuned by timing, "
-                         "3 tiles with one voxel per thread (default: form by size)")
+                         "3 tiles with one voxel per thread (default: tiles)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the roofline kernel (overrides the measured table)")
     args = ap.parse_args()

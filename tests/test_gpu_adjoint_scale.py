@@ -1,0 +1,197 @@
+"""Adjoint mode at the adjoint configuration's own scale.
+
+* 128^3 sphere pack (seed 3, radius 6 voxels, porosity 0.35), contact angle
+  = trilinear interpolation of an 8^3 control grid of angles in 0..60
+  degrees (seed 3), target = H_eps(phi_T) of a hidden control grid (seed 4),
+  200 TVD-RK3 WENO5 steps at curvature 0.2 per voxel, checkpoints every 20
+  steps: the library's gradient with respect to the controls against central
+  finite differences of the library's own forward (h = 1e-6 rad, relative
+  error <= 1e-5) on the controls with the largest gradients.
+* A 32^3 crop of the same pack (the same construction on a 32^3 box): the
+  library's loss and gradient over the 200 steps against the FP64
+  PyTorch-autograd replica of the forward model (run on the GPU through
+  torch, one checkpointed recomputation per time step)."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import qssgpu as Q
+import synthetic as S
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+STEPS, CKPT = 200, 20
+A0, B = 0.2 / 0.04, 0.04
+
+
+def _problem(gpu, n):
+    g = Q.make_grid(gpu, n)
+    v = Q.Volume(g)
+    m = S.overlapping(n, radius_vox=6.0, porosity=0.35, seed=3).mask()
+    v["mask"][...] = m
+    v["phi"][...] = S.initial_phi(m, n)
+    o = Q.default_options(gpu)
+    o.a, o.b, o.overlap, o.theta = A0, B, 0.0, 0.0
+    dx = g.dx[0]
+    dt = 0.5 / (2 * B * 3 / dx ** 2 + 2.0 / dx + abs(A0) * math.sqrt(3) / dx)
+    return g, v, o, dt
+
+
+def _axis_weights(n, nc=8):
+    """Trilinear weights (n x nc) of one axis: voxel t of the fill box sits at
+    t / (n - 1) * (nc - 1) on the control grid."""
+    t = np.arange(n) / (n - 1) * (nc - 1)
+    i0 = np.minimum(np.floor(t).astype(int), nc - 2)
+    f = t - i0
+    w = np.zeros((n, nc))
+    w[np.arange(n), i0] += 1 - f
+    w[np.arange(n), i0 + 1] += f
+    return w
+
+
+def _angles(g, ctrl, w):
+    """Ghost-box angle field from the (z, y, x) control grid."""
+    fill = np.einsum("kc,jb,ia,cba->kji", w, w, w, ctrl)
+    out = np.zeros(tuple(g.grid_dims_ghostbox[d] for d in (2, 1, 0)))
+    lo = g.ilo_fb - g.ilo_gb
+    n = fill.shape[0]
+    out[lo:lo + n, lo:lo + n, lo:lo + n] = fill
+    return out
+
+
+def _to_controls(g, grad, w):
+    lo = g.ilo_fb - g.ilo_gb
+    n = w.shape[0]
+    return np.einsum("kji,kc,jb,ia->cba", grad[lo:lo + n, lo:lo + n, lo:lo + n], w, w, w)
+
+
+def _heaviside_np(x, eps):
+    return np.where(x < -eps, 0.0, np.where(x > eps, 1.0, 0.5 + x / (2 * eps) + np.sin(math.pi * x / eps) /
+                                             (2 * math.pi)))
+
+
+def _forward(gpu, o, v, g, theta, target, dt, phi_out=None):
+    loss = C.c_double(0)
+    rc = gpu.qssgpu_forward_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(theta), Q.dptr(target), STEPS, dt,
+                                  C.byref(loss), Q.dptr(phi_out) if phi_out is not None else None)
+    assert rc == 0, gpu.qssgpu_error_string()
+    return loss.value
+
+
+def _adjoint(gpu, o, v, g, theta, target, dt):
+    loss = C.c_double(0)
+    grad = np.zeros_like(theta)
+    rc = gpu.qssgpu_adjoint_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(theta), Q.dptr(target), STEPS, dt,
+                                  CKPT, C.byref(loss), Q.dptr(grad))
+    assert rc == 0, gpu.qssgpu_error_string()
+    return loss.value, grad
+
+
+def _target(gpu, o, v, g, dt, w):
+    hidden = np.random.default_rng(4).uniform(0.0, math.radians(60.0), (8, 8, 8))
+    phiT = np.zeros(v["mask"].shape)
+    _forward(gpu, o, v, g, _angles(g, hidden, w), np.zeros(v["mask"].shape), dt, phiT)
+    return _heaviside_np(phiT, 1.5 * g.dx[0])
+
+
+def test_adjoint_128_against_finite_differences(gpu):
+    n = 128
+    g, v, o, dt = _problem(gpu, n)
+    w = _axis_weights(n)
+    target = _target(gpu, o, v, g, dt, w)
+    ctrl = np.random.default_rng(3).uniform(0.0, math.radians(60.0), (8, 8, 8))
+    loss, grad = _adjoint(gpu, o, v, g, _angles(g, ctrl, w), target, dt)
+    assert loss == _forward(gpu, o, v, g, _angles(g, ctrl, w), target, dt)
+    gc = _to_controls(g, grad, w)
+    assert np.abs(gc).max() > 0
+    h = 1e-6
+    errs = []
+    for flat in np.argsort(-np.abs(gc).ravel())[:4]:
+        c = np.unravel_index(flat, gc.shape)
+        cp, cm = ctrl.copy(), ctrl.copy()
+        cp[c] += h
+        cm[c] -= h
+        fd = (_forward(gpu, o, v, g, _angles(g, cp, w), target, dt) -
+              _forward(gpu, o, v, g, _angles(g, cm, w), target, dt)) / (2 * h)
+        errs.append((c, fd, gc[c], abs(fd - gc[c]) / abs(gc[c])))
+    assert all(e[3] <= 1e-5 for e in errs), errs
+
+
+def test_adjoint_32_crop_against_replica(gpu, oracle):
+    """The replica's operators are those of test_gpu_adjoint.py, run on the
+    GPU through torch."""
+    import test_gpu_adjoint as R
+
+    n = 32
+    g, v, o, dt = _problem(gpu, n)
+    w = _axis_weights(n)
+    target = _target(gpu, o, v, g, dt, w)
+    ctrl = np.random.default_rng(3).uniform(0.0, math.radians(60.0), (8, 8, 8))
+    loss_lib, grad = _adjoint(gpu, o, v, g, _angles(g, ctrl, w), target, dt)
+    g_lib = _to_controls(g, grad, w)
+
+    dev = torch.device("cuda")
+    coef = {k: t.to(dev) for k, t in R._coefficients(oracle, g, v).items()}
+    lo, hi = g.ilo_fb - g.ilo_gb, g.ihi_fb - g.ilo_gb
+    ng = v["mask"].shape[0]
+    mask = torch.tensor(v["mask"], device=dev)
+    phi0 = torch.tensor(v["phi"], device=dev)
+    wt = torch.tensor(w, device=dev)
+    c = torch.tensor(ctrl, device=dev, requires_grad=True)
+    theta = torch.einsum("kc,jb,ia,cba->kji", wt, wt, wt, c)
+    dx = g.dx[0]
+    eps_var = 1.5 * dx
+    m = mask[lo:hi + 1, lo:hi + 1, lo:hi + 1]
+    ag = torch.sqrt(coef["mx"] ** 2 + coef["my"] ** 2 + coef["mz"] ** 2)
+    s = m / torch.sqrt(m * m + ag * dx * ag * dx)
+    vel = R._heaviside(-m, eps_var) * A0 - s * R._heaviside(m, eps_var) * torch.cos(theta) * ag
+    assert float(torch.abs(vel).min()) >= 1e-5  # no carried normal terms in this set-up
+    V = (coef["vx"], coef["vy"], coef["vz"])
+
+    def pad(fill):
+        return torch.nn.functional.pad(fill, (lo, ng - hi - 1, lo, ng - hi - 1, lo, ng - hi - 1))
+
+    def bc(a):
+        # signed linear extrapolation of the six faces, as R._bc, on the device
+        n_ = a.shape[0]
+        mid = a[lo:hi + 1, lo:hi + 1, :]
+        left = [R._extrap(mid[:, :, lo], mid[:, :, lo + 1], lo - i) for i in range(lo)]
+        right = [R._extrap(mid[:, :, hi], mid[:, :, hi - 1], i - hi) for i in range(hi + 1, n_)]
+        mid = torch.stack(left + [mid[:, :, i] for i in range(lo, hi + 1)] + right, dim=2)
+        a = torch.cat([a[lo:hi + 1, :lo, :], mid, a[lo:hi + 1, hi + 1:, :]], dim=1)
+        a = torch.cat([torch.zeros(lo, n_, n_, dtype=a.dtype, device=a.device), a,
+                       torch.zeros(n_ - hi - 1, n_, n_, dtype=a.dtype, device=a.device)], dim=0)
+        mid = a[lo:hi + 1]
+        low = [R._extrap(mid[:, lo, :], mid[:, lo + 1, :], lo - j) for j in range(lo)]
+        high = [R._extrap(mid[:, hi, :], mid[:, hi - 1, :], j - hi) for j in range(hi + 1, n_)]
+        mid = torch.stack(low + [mid[:, j, :] for j in range(lo, hi + 1)] + high, dim=1)
+        a = torch.cat([a[:lo], mid, a[hi + 1:]], dim=0)
+        low = [R._extrap(a[lo], a[lo + 1], lo - k) for k in range(lo)]
+        high = [R._extrap(a[hi], a[hi - 1], k - hi) for k in range(hi + 1, n_)]
+        return torch.stack(low + [a[k] for k in range(lo, hi + 1)] + high, dim=0)
+
+    def step(phi, vel_):
+        fill0 = phi[lo:hi + 1, lo:hi + 1, lo:hi + 1]
+        s1 = bc(pad(fill0 + dt * R._rhs(phi, vel_, coef["b"], V, lo, hi, dx)))
+        f1 = s1[lo:hi + 1, lo:hi + 1, lo:hi + 1]
+        s2 = bc(pad(0.75 * fill0 + 0.25 * (f1 + dt * R._rhs(s1, vel_, coef["b"], V, lo, hi, dx))))
+        f2 = s2[lo:hi + 1, lo:hi + 1, lo:hi + 1]
+        s3 = bc(pad(fill0 / 3 + 2 / 3 * (f2 + dt * R._rhs(s2, vel_, coef["b"], V, lo, hi, dx))))
+        return torch.where(mask > s3, mask, s3)
+
+    phi = phi0
+    for _ in range(STEPS):
+        phi = torch.utils.checkpoint.checkpoint(step, phi, vel, use_reentrant=False)
+    H = R._heaviside(phi[lo:hi + 1, lo:hi + 1, lo:hi + 1], 1.5 * dx)
+    tgt = torch.tensor(target[lo:hi + 1, lo:hi + 1, lo:hi + 1], device=dev)
+    loss_rep = ((H - tgt) ** 2).sum()
+    loss_rep.backward()
+    g_rep = c.grad.cpu().numpy()
+    assert abs(loss_lib - loss_rep.item()) <= 1e-9 * max(1.0, abs(loss_rep.item())), (loss_lib, loss_rep.item())
+    scale = np.abs(g_rep).max()
+    assert scale > 0
+    err = np.abs(g_lib - g_rep).max()
+    assert err <= 1e-6 * scale, (err, scale)
