@@ -225,15 +225,15 @@ int qssgpu_set_weno_split(int mode);
    products and sums; -1 restores the default.  Results are identical at
    every level.  Returns the previous level. */
 int qssgpu_set_emu_level(int level);
-/* form of the WENO5 axis passes at levels >= 1: 0 sliding window in
-   registers, 1 the faces' scaled copies in shared memory and the smoothness
-   squares on the integer pipes, -1 (default) chosen by the size of the
-   launch (the second form from ~12 M fill voxels), 2 tuned: the first pass
-   over each line shape times every distinct (form, segment length) and the
-   fastest is kept for that shape (one stream synchronisation per new shape
-   and axis), 3 and 4 tiles of 16 lines x 16 (3) or 32 (4) voxels, one voxel
-   per thread, every face and centre of a tile computed once into shared
-   memory; identical results; returns the previous setting.  No
+/* form of the WENO5 axis passes at levels >= 1: -1 (default) and 3 tiles
+   of 16 lines x 16 voxels, one voxel per thread, every face and centre of a
+   tile computed once into shared memory; 4 tiles of 8 lines x 27 voxels; 0
+   sliding window in registers; 1 the window's scaled copies in shared
+   memory and the smoothness squares on the integer pipes; 2 tuned: the
+   first pass over each line shape times every distinct (form, segment
+   length), the tile form included, and the fastest is kept for that shape
+   (one stream synchronisation per new shape and axis); identical results;
+   returns the previous setting.  No
    reference counterpart: the reference's getrhs3d5th_ (3d.f:1962-2246) is a
    loop over voxels with nothing to tune. */
 int qssgpu_set_axis_variant(int variant);

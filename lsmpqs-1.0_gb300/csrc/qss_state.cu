@@ -185,7 +185,7 @@ int axis_variant() {
     const char* e = getenv("QSSGPU_AXIS_VARIANT");
     m = e ? atoi(e) : -1;
   }
-  return m < 0 ? -1 : (m > 3 ? 3 : m);
+  return m < 0 ? -1 : (m > 4 ? 4 : m);
 }
 
 int emu_level() {
@@ -473,7 +473,7 @@ int qssgpu_set_emu_level(int level) {
 
 int qssgpu_set_axis_variant(int v) {
   const int prev = axis_variant();
-  g_axis_variant = v < 0 ? -1 : (v > 3 ? 3 : v);
+  g_axis_variant = v < 0 ? -1 : (v > 4 ? 4 : v);
   return prev;
 }
 

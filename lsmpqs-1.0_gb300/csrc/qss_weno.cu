@@ -367,15 +367,27 @@ __global__ void __launch_bounds__(128, RING ? 5 : 4) k_weno_axis(AxisArgs a) {
 // 418 -> 476, 192^3 411 -> 501, 256^3 474 -> 509, 384^3 485 -> 514, 512^3
 // 497 -> 516; the FP64 pipe runs 76 % busy at 192^3 (ncu, 4 blocks per SM)
 // against 57 % for the window form.
-constexpr int TL = 16, TP = 16;
-constexpr int TF = TP + 5;  // faces s0-2 .. s0+TP+2
-constexpr int TC = TP + 3;  // centres s0-1 .. s0+TP+1
-constexpr int TE = TP + 1;  // eps+ of voxels s0-1 .. s0+TP-1
-constexpr int TNT = TL * TP;
-constexpr size_t TILE_BYTES = sizeof(double) * (8 * TF + 6 * TC + TE) * TL;
+// A tile shape: L lines (a power of two) x P voxels along the axis, handled
+// by L * NS threads; thread t works on line t % L and position slot t / L,
+// taking positions slot, slot + NS, ... in each phase.
+template <int L_, int P_, int NS_>
+struct TileGeom {
+  static constexpr int L = L_, P = P_, NS = NS_;
+  static constexpr int F = P + 5;  // faces s0-2 .. s0+P+2
+  static constexpr int C = P + 3;  // centres s0-1 .. s0+P+1
+  static constexpr int E = P + 1;  // eps+ of voxels s0-1 .. s0+P-1
+  static constexpr int NT = L * NS;
+  static constexpr size_t BYTES = sizeof(double) * (8 * F + 6 * C + E) * L;
+};
+// the default: 16 lines x 16 voxels, 256 threads (faces and centres of the
+// halo take a second round for 5 and 3 slots)
+using Tile16 = TileGeom<16, 16, 16>;
+// 8 lines x 27 voxels, 32 slots: the 32 faces take one round
+using Tile27 = TileGeom<8, 27, 32>;
+constexpr int TP = Tile16::P;
 
 // the tile kernels ask for all of the unified L1 / shared memory as shared
-// memory, so that five blocks of TILE_BYTES fit on an SM (once per process
+// memory, so that five blocks of a tile fit on an SM (once per process
 // and kernel)
 template <typename K>
 void tile_smem_attr(K kernel, bool& done) {
@@ -384,19 +396,20 @@ void tile_smem_attr(K kernel, bool& done) {
   done = true;
 }
 
-template <int AX, int EMU>
-__global__ void __launch_bounds__(TNT, 5) k_weno_tile(AxisArgs a) {
+template <int AX, int EMU, typename G>
+__global__ void __launch_bounds__(G::NT, 5) k_weno_tile(AxisArgs a) {
   if (a.ctl && !a.ctl->active) return;
+  constexpr int TL = G::L, TP = G::P, NS = G::NS, TF = G::F, TC = G::C, TE = G::E;
   const Box& b = a.b;
   // faces: v, w, 3v and the five scaled copies; centres: six smoothness
   // indicators; eps+ per voxel; all [field][position][line], in dynamic
-  // shared memory (TILE_BYTES)
+  // shared memory (G::BYTES)
   extern __shared__ double tile_smem[];
   auto sf = reinterpret_cast<double(*)[TF][TL]>(tile_smem);
   auto sc = reinterpret_cast<double(*)[TC][TL]>(tile_smem + 8 * TF * TL);
   auto se = reinterpret_cast<double(*)[TL]>(tile_smem + (8 * TF + 6 * TC) * TL);
-  const int line = threadIdx.x & (TL - 1);
-  const int slot = threadIdx.x >> 4;  // 0..TP-1: position within a round
+  const int line = threadIdx.x % TL;
+  const int slot = threadIdx.x / TL;  // 0..NS-1: position within a round
   int p, q, lo, hi, plast_line;
   if (AX == 0) {
     p = b.jlo + blockIdx.x * TL + line;  // j
@@ -433,7 +446,7 @@ __global__ void __launch_bounds__(TNT, 5) k_weno_tile(AxisArgs a) {
   };
 
   // faces m = s0-2+f (between voxels m-1 and m)
-  for (int f = slot; f < TF; f += TP) {
+  for (int f = slot; f < TF; f += NS) {
     const int m = s0 - 2 + f;
     const Face fc = make_face_e<EMU>(ld(m), ld(m - 1), a.inv);
     sf[0][f][line] = fc.v;
@@ -447,7 +460,7 @@ __global__ void __launch_bounds__(TNT, 5) k_weno_tile(AxisArgs a) {
   }
   __syncthreads();
   // centres s0-1+c from faces c, c+1, c+2; eps+ of voxel s0-1+e from faces e .. e+4
-  for (int c = slot; c < TC; c += TP) {
+  for (int c = slot; c < TC; c += NS) {
     Face fa{}, fb{}, fd{};
     fa.v = sf[0][c][line];
     fa.t3 = sf[2][c][line];
@@ -468,7 +481,7 @@ __global__ void __launch_bounds__(TNT, 5) k_weno_tile(AxisArgs a) {
   __syncthreads();
   const int t = slot;
   const int i = s0 + t;
-  if (!line_ok || i > hi) return;
+  if (!line_ok || t >= TP || i > hi) return;
   auto F = [&](int field, int f) -> double { return sf[field][f][line]; };
   // plus: v1..v5 = faces i+3, i+2, i+1, i, i-1 (tile faces t+5 .. t+1)
   const double pp1_ = (F(3, t + 5) - F(4, t + 4)) + F(5, t + 3);
@@ -677,27 +690,28 @@ int default_seg_len(int var, int64_t lines, int along) {
   return var ? seg_len_for(lines, along, 16, along / 64) : seg_len_for(lines, along, 8, (along + SEG - 1) / SEG);
 }
 
-template <int EMU>
+template <int EMU, typename G>
 void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
-  const dim3 gt((lanes + TL - 1) / TL, other, (along + TP - 1) / TP);
+  const dim3 gt((lanes + G::L - 1) / G::L, other, (along + G::P - 1) / G::P);
   static bool done[3] = {false, false, false};
   if (ax == 0) {
-    tile_smem_attr(k_weno_tile<0, EMU>, done[0]);
-    k_weno_tile<0, EMU><<<gt, TNT, TILE_BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<0, EMU, G>, done[0]);
+    k_weno_tile<0, EMU, G><<<gt, G::NT, G::BYTES, s>>>(a);
   } else if (ax == 1) {
-    tile_smem_attr(k_weno_tile<1, EMU>, done[1]);
-    k_weno_tile<1, EMU><<<gt, TNT, TILE_BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<1, EMU, G>, done[1]);
+    k_weno_tile<1, EMU, G><<<gt, G::NT, G::BYTES, s>>>(a);
   } else {
-    tile_smem_attr(k_weno_tile<2, EMU>, done[2]);
-    k_weno_tile<2, EMU><<<gt, TNT, TILE_BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<2, EMU, G>, done[2]);
+    k_weno_tile<2, EMU, G><<<gt, G::NT, G::BYTES, s>>>(a);
   }
 }
 
 template <int EMU>
 void launch_axis(cudaStream_t s, int ax, int var, AxisArgs a, int lanes, int other, int along, int len) {
   a.seg_len = len;
-  if (var == 3 && EMU != 0) {
-    launch_tile<EMU>(s, ax, a, lanes, other, along);
+  if (var >= 3 && EMU != 0) {
+    if (var == 4) launch_tile<EMU, Tile27>(s, ax, a, lanes, other, along);
+    else launch_tile<EMU, Tile16>(s, ax, a, lanes, other, along);
     return;
   }
   dim3 g((lanes + 127) / 128, other, (along + len - 1) / len);
@@ -783,7 +797,7 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     // kept selectable, the shared-memory one is the faster from ~12 M fill
     // voxels on (register / shared-memory form, M voxel-steps/s: 128^3
     // 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
-    int var = mode == 0 || mode == 1 || mode == 3 ? mode : 3;
+    int var = mode == 0 || mode == 1 || mode == 3 || mode == 4 ? mode : 3;
     if (mode == 2) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
     int len = EMU == 0 ? SEG : default_seg_len(var, (int64_t)lanes * other, along);
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};

@@ -119,14 +119,14 @@ def test_host_side_argument_checks(lib):
 
 def test_axis_variant_settings(lib):
     """The axis-pass form setting takes -1 (default: tiles), 0, 1 (window
-    forms), 2 (tuned) and 3 (tiles), clamps larger values to 3, returns the
-    previous setting, and the tuned shape table starts empty and can be
-    cleared."""
+    forms), 2 (tuned), 3 and 4 (tiles of 16 x 16 and 8 x 27), clamps larger
+    values to 4, returns the previous setting, and the tuned shape table
+    starts empty and can be cleared."""
     L = Q.load(Q.GPU_LIB)
     prev = L.qssgpu_set_axis_variant(2)
     try:
         assert L.qssgpu_set_axis_variant(7) == 2
-        assert L.qssgpu_set_axis_variant(0) == 3
+        assert L.qssgpu_set_axis_variant(0) == 4
         assert L.qssgpu_set_axis_variant(-5) == 0
     finally:
         L.qssgpu_set_axis_variant(prev)

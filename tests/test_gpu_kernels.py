@@ -74,7 +74,7 @@ def test_rhs_slab_and_tiny_speed(gpu, oracle, name, var):
 
 
 @pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 0), (1, 1, 1), (1, 2, 0),
-                                               (1, 2, 1), (1, 1, 2), (1, 2, 2), (1, 1, 3), (1, 2, 3)])
+                                               (1, 2, 1), (1, 1, 2), (1, 2, 2), (1, 1, 3), (1, 2, 3), (1, 2, 4)])
 @pytest.mark.parametrize("small", [0.0, 0.2])
 def test_weno5_split_and_fused(gpu, oracle, split, emu, variant, small):
     """The WENO5 stage runs as one fused kernel (split 0) or as one kernel per
