@@ -217,6 +217,10 @@ static void destroy_volume(DevVolume* v) {
   for (cudaEvent_t e : v->ev_pool) cudaEventDestroy(e);
   if (v->h_ctl) cudaFreeHost(v->h_ctl);
   if (v->h_scal) cudaFreeHost(v->h_scal);
+  for (cudaStream_t x : v->xfer)
+    if (x) cudaStreamDestroy(x);
+  for (cudaEvent_t e : v->xfer_ev)
+    if (e) cudaEventDestroy(e);
   if (v->stream) cudaStreamDestroy(v->stream);
   delete v;
 }
@@ -262,6 +266,8 @@ static void alloc_volume(DevVolume* v) {
   const Box& b = v->box;
   const int64_t n = v->n;
   QSS_CK(cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking));
+  for (auto& x : v->xfer) QSS_CK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  for (auto& e : v->xfer_ev) QSS_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   double** reals[] = {&v->phi, &v->s1, &v->s2, &v->phi_prev, &v->mask, &v->mask_w, &v->mask_nw,
                       &v->mask_disconn, &v->mask_x, &v->mask_y, &v->mask_z, &v->phi_extra,
                       &v->vel_n, &v->bcoef, &v->vx, &v->vy, &v->vz, &v->scratch,
@@ -414,6 +420,14 @@ void start_prefault(DevVolume& v, const QSS_DataArrays* p, std::initializer_list
 void download_dirty(DevVolume& v, QSS_DataArrays* p) {
   PhaseTimer pt(v, PH_DOWNLOAD);
   v.prefault.join();
+  // the copies go round-robin to the volume's stream and its two transfer
+  // streams, which start after everything queued so far and are joined
+  // before the return: three copy engines move the arrays at once
+  QSS_CK(cudaEventRecord(v.xfer_ev[0], v.stream));
+  for (cudaStream_t x : v.xfer) QSS_CK(cudaStreamWaitEvent(x, v.xfer_ev[0], 0));
+  const cudaStream_t lanes[3] = {v.stream, v.xfer[0], v.xfer[1]};
+  int next = 0;
+  auto lane = [&]() { return lanes[next++ % 3]; };
   // arrays the reference leaves zero: copied from a zeroed device buffer (the
   // reinitialisation scratch, free once the call's work is queued) by the
   // copy engine, which writes host memory faster than a CPU memset
@@ -427,9 +441,14 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
     }
     if (v.zero_on_return[a]) {
       const size_t bytes = (size_t)v.n * elem_size(w);  // at most n doubles
-      if (!zeroed) QSS_CK(cudaMemsetAsync(v.r_next, 0, (size_t)v.n * sizeof(double), v.stream));
+      if (!zeroed) {
+        // cleared on the volume's stream, then made visible to the other two
+        QSS_CK(cudaMemsetAsync(v.r_next, 0, (size_t)v.n * sizeof(double), v.stream));
+        QSS_CK(cudaEventRecord(v.xfer_ev[0], v.stream));
+        for (cudaStream_t x : v.xfer) QSS_CK(cudaStreamWaitEvent(x, v.xfer_ev[0], 0));
+      }
       zeroed = true;
-      QSS_CK(cudaMemcpyAsync(h, v.r_next, bytes, cudaMemcpyDeviceToHost, v.stream));
+      QSS_CK(cudaMemcpyAsync(h, v.r_next, bytes, cudaMemcpyDeviceToHost, lane()));
     } else if (v.dirty[a]) {
       void* d = dev_ptr(v, w);
       if (!d) continue;
@@ -438,17 +457,22 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
         // ghost values must survive, so only fill-box rows travel
         const Box& b = v.box;
         const size_t pitch = (size_t)b.nx * sizeof(double);
+        const cudaStream_t st = lane();
         for (int k = b.klo; k <= b.khi; k++) {
           const size_t off = (size_t)b.idx(b.ilo, b.jlo, k) * sizeof(double);
           QSS_CK(cudaMemcpy2DAsync((char*)h + off, pitch, (const char*)d + off, pitch,
                                    (size_t)b.fbx() * sizeof(double), (size_t)b.fby(), cudaMemcpyDeviceToHost,
-                                   v.stream));
+                                   st));
         }
       } else {
-        QSS_CK(cudaMemcpyAsync(h, d, (size_t)v.n * elem_size(w), cudaMemcpyDeviceToHost, v.stream));
+        QSS_CK(cudaMemcpyAsync(h, d, (size_t)v.n * elem_size(w), cudaMemcpyDeviceToHost, lane()));
       }
     }
     v.dirty[a] = v.zero_on_return[a] = false;
+  }
+  for (int x = 0; x < 2; x++) {
+    QSS_CK(cudaEventRecord(v.xfer_ev[1 + x], v.xfer[x]));
+    QSS_CK(cudaStreamWaitEvent(v.stream, v.xfer_ev[1 + x], 0));
   }
   QSS_CK(cudaStreamSynchronize(v.stream));
 }

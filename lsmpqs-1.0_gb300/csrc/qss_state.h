@@ -85,6 +85,10 @@ struct DevVolume {
   int64_t n = 0;
   int64_t nfb = 0;
   cudaStream_t stream = nullptr;
+  // two more streams and their events for the downloads on return, which then
+  // run on several copy engines at once (created with the volume)
+  cudaStream_t xfer[2] = {nullptr, nullptr};
+  cudaEvent_t xfer_ev[3] = {nullptr, nullptr, nullptr};
   // level set and the two stage buffers
   double *phi = nullptr, *s1 = nullptr, *s2 = nullptr, *phi_prev = nullptr;
   double *mask = nullptr, *mask_w = nullptr, *mask_nw = nullptr, *mask_disconn = nullptr;

@@ -379,12 +379,13 @@ struct TileGeom {
   static constexpr int NT = L * NS;
   static constexpr size_t BYTES = sizeof(double) * (8 * F + 6 * C + E) * L;
 };
-// the default: 16 lines x 16 voxels, 256 threads (faces and centres of the
-// halo take a second round for 5 and 3 slots)
+// 16 lines x 16 voxels, 256 threads (faces and centres of the halo take a
+// second round for 5 and 3 slots)
 using Tile16 = TileGeom<16, 16, 16>;
-// 8 lines x 27 voxels, 32 slots: the 32 faces take one round
+// 8 lines x 27 voxels, 32 slots, 256 threads: the 32 faces take one round,
+// the 30 centres one (2 slots idle), the 27 voxels one (5 slots idle); lines
+// of a multiple of 27 voxels lose nothing to the last tile
 using Tile27 = TileGeom<8, 27, 32>;
-constexpr int TP = Tile16::P;
 
 // the tile kernels ask for all of the unified L1 / shared memory as shared
 // memory, so that five blocks of a tile fit on an SM (once per process
@@ -749,7 +750,8 @@ bool tune_axis(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, 
     for (const auto& d : cand) seen = seen || d == c;
     if (!seen) cand.push_back(c);
   };
-  add(3, TP);  // the tile form (its segment is the tile)
+  add(3, Tile16::P);  // the tile forms (their segment is the tile)
+  add(4, Tile27::P);
   for (int v = 0; v < 2; v++) {
     add(v, default_seg_len(v, lines, along));
     for (int64_t waves : {2, 4, 8, 16, 32}) add(v, seg_len_for(lines, along, waves, (along + SEG - 1) / SEG));
@@ -784,6 +786,15 @@ bool tune_axis(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, 
   return ok && active;
 }
 
+// The default tile: 8 x 27 where the line splits into 27-voxel tiles with at
+// most 2 % of the last tile unused, else 16 x 16 (whole WENO5 stage on GB300,
+// M voxel-steps/s, 16 x 16 / 8 x 27: 512^3 516 / 532 (1.2 % unused),
+// 192^3 501 / 485 (12.5 % unused)).
+int tile_form_for(int along) {
+  const int tiles = (along + Tile27::P - 1) / Tile27::P;
+  return (int64_t)tiles * Tile27::P * 50 <= (int64_t)along * 51 ? 4 : 3;
+}
+
 template <int EMU>
 void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[3], double* const dp[3],
              double* const dm[3], const Ctl* ctl) {
@@ -792,12 +803,12 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
     const int along = ax == 0 ? b.fbx() : (ax == 1 ? b.fby() : b.fbz());
     const int lanes = ax == 0 ? b.fby() : b.fbx();
     const int other = ax == 2 ? b.fby() : b.fbz();
-    // by default the tile form, the fastest at every size measured on GB300
-    // (64^3 .. 512^3, see k_weno_tile); of the two window forms, which are
+    // by default a tile form (tile_form_for), the fastest at every size
+    // measured on GB300 (64^3 .. 512^3, see k_weno_tile); of the two window forms, which are
     // kept selectable, the shared-memory one is the faster from ~12 M fill
     // voxels on (register / shared-memory form, M voxel-steps/s: 128^3
     // 420 / 383, 192^3 411 / 385, 256^3 458 / 473, 512^3 469 / 488)
-    int var = mode == 0 || mode == 1 || mode == 3 || mode == 4 ? mode : 3;
+    int var = mode == 0 || mode == 1 || mode == 3 || mode == 4 ? mode : tile_form_for(along);
     if (mode == 2) var = (int64_t)lanes * other * along >= kRingVoxels ? 1 : 0;
     int len = EMU == 0 ? SEG : default_seg_len(var, (int64_t)lanes * other, along);
     AxisArgs a{b, phi, dp[ax], dm[ax], invs[ax], ctl, len};
@@ -933,7 +944,8 @@ int qssgpu_axis_tuning_load(const char* path) {
     char tail;
     ok = sscanf(c, "%d %d %d %d %d %d %d %c", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &tail) == 7 &&
          v[0] >= 1 && v[0] <= 2 && v[1] >= 0 && v[1] <= 2 && v[2] > 0 && v[3] > 0 && v[4] > 0 &&
-         (v[5] == 0 || v[5] == 1 || v[5] == 3) && v[6] >= 1 && (v[5] == 3 ? v[6] == qss::TP : v[6] <= v[4]);
+         (v[5] == 0 || v[5] == 1 || v[5] == 3 || v[5] == 4) && v[6] >= 1 &&
+         (v[5] == 3 ? v[6] == qss::Tile16::P : v[5] == 4 ? v[6] == qss::Tile27::P : v[6] <= v[4]);
     if (ok) rows.push_back({qss::TuneKey{v[0], v[1], v[2], v[3], v[4]}, std::array<int, 2>{v[5], v[6]}});
   }
   fclose(fp);

@@ -170,8 +170,9 @@ def test_tuned_axis_shapes(gpu, oracle):
     r = np.array(rows[:7 * n]).reshape(n, 7)
     assert sorted(r[:, 1].tolist()) == [0, 1, 2]
     assert set(r[:, 0].tolist()) == {2}
-    assert set(r[:, 5].tolist()) <= {0, 1, 3}
-    assert ((r[:, 6] >= 1) & (r[:, 6] <= np.where(r[:, 5] == 3, 16, r[:, 4]))).all()
+    assert set(r[:, 5].tolist()) <= {0, 1, 3, 4}
+    seg_max = np.where(r[:, 5] == 3, 16, np.where(r[:, 5] == 4, 27, r[:, 4]))
+    assert ((r[:, 6] >= 1) & (r[:, 6] <= seg_max)).all()
     gpu.qssgpu_axis_tuning_reset()
     assert gpu.qssgpu_axis_tuning(None, 0) == 0
 
