@@ -600,14 +600,18 @@ __device__ __forceinline__ double impose3_e(double v, int64_t idx, const ImposeA
   return v;
 }
 
+// One block: 32 (i) x 4 (j) voxels of one k plane; each warp covers an 8 x 4
+// patch of them, so that the warps that lie wholly where the curvature
+// coefficient is zero (inside the grains) skip the curvature term together.
 template <int STAGE, bool FINAL, int EMU>
 __global__ void __launch_bounds__(128) k_weno_combine(CombineArgs a) {
   if (STAGE != 0 && !a.ctl->active) return;
   using Q = Ar<EMU>;
   const Box& b = a.b;
-  const int i = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = b.jlo + blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = b.klo + blockIdx.z * blockDim.z + threadIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = b.ilo + blockIdx.x * 32 + 8 * warp + (lane & 7);
+  const int j = b.jlo + blockIdx.y * 4 + (lane >> 3);
+  const int k = b.klo + blockIdx.z;
   if (i > b.ihi || j > b.jhi || k > b.khi) return;
   const int64_t idx = b.idx(i, j, k);
   double pp[3], pm[3];
@@ -646,7 +650,13 @@ __global__ void __launch_bounds__(128) k_weno_combine(CombineArgs a) {
     az = (vz >= 0) ? pm[2] : pp[2];
   }
   const double temp_vel = -(vx * ax + vy * ay + vz * az);
-  const double temp_curv = a.c.b[idx] * curvature_e<EMU>(a.phi_in, b, idx, a.fac);
+  // b * kappa is +-0 where b is +0, and (temp_norm + (+-0)) equals
+  // (temp_norm + 0.0) unless temp_norm is -0: there the curvature (finite:
+  // its denominator is at least 1e-5) changes nothing and is skipped
+  const double bco = a.c.b[idx];
+  const double temp_curv = (qss_emu::bits(bco) == 0 && qss_emu::bits(temp_norm) != qss_emu::kSign)
+                               ? 0.0
+                               : bco * curvature_e<EMU>(a.phi_in, b, idx, a.fac);
   const double rhs = temp_norm + temp_curv + temp_vel;
   double out;
   if (STAGE == 0) {
@@ -877,7 +887,7 @@ void launch_weno_combine(cudaStream_t s, int stage, bool final_stage, const Box&
   a.c = c;
   a.im = im;
   a.ctl = ctl;
-  const dim3 blk(32, 4, 1);
+  const dim3 blk(128, 1, 1);
   const dim3 g((b.fbx() + 31) / 32, (b.fby() + 3) / 4, b.fbz());
   cudaEvent_t e0 = stage != 0 ? prof_open(s) : nullptr;
   switch (emu_level()) {

@@ -73,6 +73,35 @@ def test_rhs_slab_and_tiny_speed(gpu, oracle, name, var):
         assert a[1] == o[1]
 
 
+@pytest.mark.parametrize("emu", [0, 2])
+def test_weno5_rhs_zero_curvature_coefficient(gpu, oracle, emu):
+    """Where the curvature coefficient is +0 the combine kernel skips the
+    curvature, except where the normal term is -0 (here: a flat patch of the
+    level set under a negative speed), where b * kappa could decide the sign
+    of a zero: the right-hand side must equal the oracle's bit for bit, signs
+    of zeros included."""
+    g, _ = pack_case(oracle, N)
+    phi, vel, b, vx, vy, vz = _fields(g, 11)
+    nz, ny, nx = phi.shape
+    b[:, :, : nx // 2] = 0.0  # half the box without curvature
+    phi[4:14, 4:14, 3:12] = 0.37  # a flat patch: zero one-sided derivatives inside it
+    vel[4:14, 4:14, 3:12] = -0.5  # ... and a negative speed: temp_norm = -0
+    vx[4:14, 4:14, 3:12] = 0.0
+    vy[4:14, 4:14, 3:12] = 0.0
+    vz[4:14, 4:14, 3:12] = 0.0
+    prev_emu = gpu.qssgpu_set_emu_level(emu)
+    try:
+        a = _run_rhs(gpu, "getrhs3d5th_", True, g, phi, vel, b, vx, vy, vz)
+    finally:
+        gpu.qssgpu_set_emu_level(prev_emu)
+    o = _run_rhs(oracle, "getrhs3d5th_", True, g, phi, vel, b, vx, vy, vz)
+    Q.check(gpu)
+    assert np.array_equal(a[0].view(np.int64), o[0].view(np.int64))
+    assert a[1] == o[1]
+    # the flat patch gives exact zeros (normal, advection and curvature terms all zero)
+    assert (o[0][7:11, 7:11, 6:9] == 0.0).all()
+
+
 @pytest.mark.parametrize("split,emu,variant", [(0, 2, -1), (1, 0, -1), (1, 1, 0), (1, 1, 1), (1, 2, 0),
                                                (1, 2, 1), (1, 1, 2), (1, 2, 2), (1, 1, 3), (1, 2, 3), (1, 2, 4)])
 @pytest.mark.parametrize("small", [0.0, 0.2])
