@@ -228,9 +228,11 @@ N_KINDS = 5
 # x pass 7.74 GB, y pass 3.40 GB, z pass 3.37 GB, combine 14.22 GB for 134.2 M
 # voxels; the fused kernel was not captured
 TRAFFIC_BYTES_PER_VOXEL = {1: 57.7, 2: 25.3, 3: 25.1, 4: 105.9}
-# the same for the tile form of the axis passes (the default), measured at
-# 192^3 and scaled per voxel
-TRAFFIC_BYTES_PER_VOXEL_TILE = {}
+# the same for the 16 x 16 tile form of the axis passes and the combine kernel,
+# measured at 256^3 with ncu (one kernel and at most three launches per
+# capture): x pass 474.2 MB, y 363.9 MB, z 362.2 MB, combine 2470.3 MB for
+# 16.78 M voxels
+TRAFFIC_BYTES_PER_VOXEL_TILE = {1: 28.3, 2: 21.7, 3: 21.6, 4: 147.2}
 # algorithmic HBM bytes per voxel-step (each array touched once per stage):
 # stage 1 phi + 5 coefficients -> phi1, stage 2 phi1 + phi + 5 coeff -> phi2,
 # stage 3 phi2 + phi + 5 coeff + 3 masks -> phi1, phi
@@ -329,7 +331,7 @@ def gpu_arm(args, dist: Dist):
     tile = top in (1, 2, 3) and not window
     if tile or (top == 4 and not window):
         traffic_table = dict(TRAFFIC_BYTES_PER_VOXEL_TILE)
-        traffic_unit = "bytes per launch (ncu at 192^3, scaled per voxel to this size)"
+        traffic_unit = "bytes per launch (ncu at 256^3 with 16 x 16 tiles, scaled per voxel to this size)"
     else:
         traffic_table = TRAFFIC_BYTES_PER_VOXEL
         traffic_unit = "bytes per launch (ncu at 512^3, scaled per voxel to this size)"
