@@ -104,11 +104,15 @@ struct AdjPointArgs {
 // curvature term b kappa (3d.f:2337-2379) with respect to its ten central
 // differences, each times the voxel's adjoint weight.  Voxels whose normal
 // term is carried from an earlier voxel leave that term to k_adj_carry.
+// A block of 32 x 4 threads covers 32 (i) x 4 (j) voxels; each warp an 8 x 4
+// patch of them, so that warps inside the grains (b = 0) skip the curvature
+// partials together.
 __global__ void __launch_bounds__(128) k_adj_point(AdjPointArgs a) {
   const Box& b = a.b;
-  const int i = b.ilo + blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = b.jlo + blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = b.klo + blockIdx.z * blockDim.z + threadIdx.z;
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int i = b.ilo + blockIdx.x * 32 + 8 * warp + (lane & 7);
+  const int j = b.jlo + blockIdx.y * 4 + (lane >> 3);
+  const int k = b.klo + blockIdx.z;
   if (i > b.ihi || j > b.jhi || k > b.khi) return;
   const int64_t q = b.idx(i, j, k);
   const double w = a.coef_l * a.lam_in[q];
@@ -144,7 +148,8 @@ __global__ void __launch_bounds__(128) k_adj_point(AdjPointArgs a) {
     const double phy = (phi[q + st[1]] - phi[q - st[1]]) * fy;
     const double phz = (phi[q + st[2]] - phi[q - st[2]]) * fz;
     const double grad = __dadd_rn(__dadd_rn(__dmul_rn(phx, phx), __dmul_rn(phy, phy)), __dmul_rn(phz, phz));
-    if (w != 0.0 && qss_emu::bits(grad) >= qss_emu::bits(1.e-5)) {  // grad >= 1e-5 (a sum of squares)
+    // nothing flows through b kappa where b is zero (grain interiors)
+    if (w != 0.0 && a.bcoef[q] != 0.0 && qss_emu::bits(grad) >= qss_emu::bits(1.e-5)) {  // grad >= 1e-5
       const double cc = phi[q];
       const double pxx = (phi[q + 2 * st[0]] + phi[q - 2 * st[0]] - 2 * cc) * a.f2[0];
       const double pyy = (phi[q + 2 * st[1]] + phi[q - 2 * st[1]] - 2 * cc) * a.f2[1];
