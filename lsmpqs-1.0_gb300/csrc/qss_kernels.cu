@@ -513,17 +513,18 @@ __device__ __forceinline__ double reinit_rhs_diffs(double cc, double p0, double 
 // the difference (phi(c + e) - phi(c)) inv is the plus difference of c and
 // the minus difference of c + e, the same operation on the same operands.
 // A block of 4 warps covers 32 (i) x 4 (j) voxels, each warp an 8 x 4 patch
-// (x neighbours one lane apart, y neighbours eight), and walks kRWalk planes
+// (x neighbours one lane apart, y neighbours eight), and walks `walk` planes
 // along k carrying the z difference; lanes on the patch's low edges and the
 // first plane compute their minus difference themselves.  Per voxel about
-// 3.4 differences instead of 6.
-constexpr int kRWalk = 16;
+// 3.4 differences instead of 6 for a walk of 16 planes.  Short walks keep
+// small boxes' grids large enough to fill the GPU (see reinit_launch).
+constexpr int kRWalkMax = 16;
 
 __global__ void __launch_bounds__(128) k_reinit_walk(Box b, const double* __restrict__ data,
                                                      const double* __restrict__ phi0,
                                                      const double* __restrict__ distance0, double* __restrict__ next,
                                                      double dt_r, Inv inv, double max_dx, int rhs_only,
-                                                     uint64_t far_bits) {
+                                                     uint64_t far_bits, int walk) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int li = lane & 7, lj = lane >> 3;
   const int i_raw = b.ilo + blockIdx.x * 32 + 8 * warp + li;
@@ -532,8 +533,8 @@ __global__ void __launch_bounds__(128) k_reinit_walk(Box b, const double* __rest
   // lanes past the fill box work on its last row/column (in the box), store nothing
   const int i = i_raw <= b.ihi ? i_raw : b.ihi;
   const int j = j_raw <= b.jhi ? j_raw : b.jhi;
-  const int k0 = b.klo + blockIdx.z * kRWalk;
-  const int k1 = k0 + kRWalk - 1 < b.khi ? k0 + kRWalk - 1 : b.khi;
+  const int k0 = b.klo + blockIdx.z * walk;
+  const int k1 = k0 + walk - 1 < b.khi ? k0 + walk - 1 : b.khi;
   const int64_t sy = b.sy(), sz = b.sz();
   auto scale = [](double d, double f) -> double { return qss_emu::mul(d, f); };
   int64_t c = b.idx(i, j, k0);
@@ -1032,8 +1033,13 @@ static void reinit_launch(cudaStream_t s, const Box& b, const double* data, cons
   const int lvl = emu_level();
   const dim3 grid = fb_grid(b, kBlk3);
   if (lvl >= 2 && reinit_walk()) {
-    const dim3 gw((b.fbx() + 31) / 32, (b.fby() + 3) / 4, (b.fbz() + kRWalk - 1) / kRWalk);
-    k_reinit_walk<<<gw, 128, 0, s>>>(b, data, phi0, distance0, out, dt_r, inv, max_dx, rhs_only, far_bits);
+    // planes per thread: up to kRWalkMax while the grid keeps ~16 blocks per SM
+    const int64_t xy = (int64_t)((b.fbx() + 31) / 32) * ((b.fby() + 3) / 4);
+    int64_t walk = xy * b.fbz() / (152 * 16);
+    walk = walk < 1 ? 1 : (walk > kRWalkMax ? kRWalkMax : walk);
+    const dim3 gw((b.fbx() + 31) / 32, (b.fby() + 3) / 4, (unsigned)((b.fbz() + walk - 1) / walk));
+    k_reinit_walk<<<gw, 128, 0, s>>>(b, data, phi0, distance0, out, dt_r, inv, max_dx, rhs_only, far_bits,
+                                     (int)walk);
   } else if (lvl >= 2)
     k_reinit_step<2><<<grid, kBlk3, 0, s>>>(b, data, phi0, distance0, out, dt_r, inv, max_dx, rhs_only, far_bits);
   else if (lvl == 1)

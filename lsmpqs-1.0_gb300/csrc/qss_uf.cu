@@ -194,21 +194,52 @@ __global__ void __launch_bounds__(kTileThreads) k_uf_tile(Box b, const unsigned 
 // same two tile components, so the lanes of a warp first agree on distinct
 // (parent, parent) pairs and only one lane per pair unites them (the parents
 // are in the same sets as the voxels).
+// Preceding offsets have di, dj in {-1, 0, 1} and dk in {-1, 0}, so only the
+// voxels of the tile's bottom plane (lk = 0) and of the ring li or lj in
+// {0, kTile-1} of every other plane have one outside the tile: 64 + 7 x 28 =
+// 260 of the 512.  face_voxel(f) enumerates them.
+constexpr int kFaceN = kTile * kTile + (kTile - 1) * 4 * (kTile - 1);
+
+__device__ __forceinline__ void face_voxel(int f, int& li, int& lj, int& lk) {
+  if (f < kTile * kTile) {
+    lk = 0;
+    li = f % kTile;
+    lj = f / kTile;
+    return;
+  }
+  const int g = f - kTile * kTile, ring = 4 * (kTile - 1);
+  lk = 1 + g / ring;
+  const int r = g % ring;
+  if (r < kTile) {
+    lj = 0;
+    li = r;
+  } else if (r < 2 * kTile) {
+    lj = kTile - 1;
+    li = r - kTile;
+  } else if (r < 3 * kTile - 2) {
+    li = 0;
+    lj = 1 + (r - 2 * kTile);
+  } else {
+    li = kTile - 1;
+    lj = 1 + (r - (3 * kTile - 2));
+  }
+}
+
 __global__ void __launch_bounds__(kTileThreads) k_uf_cross(Box b, const unsigned char* __restrict__ bin, int* parent,
                                                            Ctl* ctl) {
   const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile, z0 = blockIdx.z * kTile;
   const unsigned lane = threadIdx.x & 31u;
   int err = 0;
-  // every thread runs kTileN / kTileThreads iterations (warp-uniform loop)
-  for (int l = threadIdx.x; l < kTileN; l += kTileThreads) {
-    const int li = l % kTile, lj = (l / kTile) % kTile, lk = l / (kTile * kTile);
-    // preceding offsets have di, dj in {-1, 0, 1} and dk in {-1, 0}: only
-    // these voxels have one outside the tile
-    const bool face = li == 0 || li == kTile - 1 || lj == 0 || lj == kTile - 1 || lk == 0;
+  // the tile's face voxels, one per thread (warp-uniform loop: a warp runs a
+  // round while its first voxel exists)
+  for (int base = threadIdx.x - (int)lane; base < kFaceN; base += kTileThreads) {
+    const int l = base + (int)lane;
+    int li = 0, lj = 0, lk = 0;
+    if (l < kFaceN) face_voxel(l, li, lj, lk);
     const int i = x0 + li, j = y0 + lj, k = z0 + lk;
-    const bool in = i < b.nx && j < b.ny && k < b.nz;
+    const bool in = l < kFaceN && i < b.nx && j < b.ny && k < b.nz;
     const int64_t q = in ? b.idx(i, j, k) : 0;
-    const bool fg = face && in && bin[q];
+    const bool fg = in && bin[q];
 #pragma unroll 1
     for (int m = 0; m < 13; m++) {
       int di, dj, dk;
