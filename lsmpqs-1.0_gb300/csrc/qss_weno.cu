@@ -30,6 +30,7 @@
 //   E(c) = 1/4 (v(c+1) - v(c-1))^2              second term of S2+(c-1) and S2-(c)
 //   eps-(i) = eps+(i-1)                          (same five squares, max is exact)
 #include <array>
+#include <cstdlib>
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -110,6 +111,22 @@ __device__ __forceinline__ Face make_face_e(double hi, double lo, double inv) {
   return f;
 }
 
+// the face with its square and 3v on the integer pipes as well (tile form)
+__device__ __forceinline__ Face make_face_i(double hi, double lo, double inv) {
+  using qss_emu::mul;
+  Face f;
+  const double d = hi - lo;
+  f.v = d * inv;
+  f.w = mul(f.v, f.v);
+  f.t3 = mul(3.0, f.v);
+  f.c13 = mul(kC13, f.v);
+  f.c76 = mul(kC76, f.v);
+  f.c116 = mul(kC116, f.v);
+  f.c16 = mul(kC16, f.v);
+  f.c56 = mul(kC56, f.v);
+  return f;
+}
+
 struct Centre {
   double s1p, s2p, s3p, s1m, s2m, s3m;
 };
@@ -158,7 +175,7 @@ __device__ __forceinline__ double eps_of(double w1, double w2, double w3, double
 
 // weights and combination of one side (3d.f:1996-2005) given the candidate
 // stencils and smoothness indicators
-template <int EMU, bool SQ>
+template <int EMU, bool SQ, bool MULC = false>
 __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, double S1, double S2, double S3,
                                                double eps) {
   using Q = Ar<EMU>;
@@ -174,6 +191,8 @@ __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, 
   a1 = Q::mul2(a1, inv_sum_a);
   a2 = Q::mul2(a2, inv_sum_a);
   a3 = Q::mul2(a3, inv_sum_a);
+  // the combination's products on the integer pipes too when MULC
+  if (MULC) return Q::mul2(a1, p1) + Q::mul2(a2, p2) + Q::mul2(a3, p3);
   return a1 * p1 + a2 * p2 + a3 * p3;
 }
 
@@ -397,7 +416,9 @@ void tile_smem_attr(K kernel, bool& done) {
   done = true;
 }
 
-template <int AX, int EMU, typename G>
+// MUL bit 0: the faces' squares and 3v on the integer pipes; bit 1: the
+// weights' products with the candidate stencils as well (EMU 2 only)
+template <int AX, int EMU, typename G, int MUL = 0>
 __global__ void __launch_bounds__(G::NT, 5) k_weno_tile(AxisArgs a) {
   if (a.ctl && !a.ctl->active) return;
   constexpr int TL = G::L, TP = G::P, NS = G::NS, TF = G::F, TC = G::C, TE = G::E;
@@ -449,7 +470,8 @@ __global__ void __launch_bounds__(G::NT, 5) k_weno_tile(AxisArgs a) {
   // faces m = s0-2+f (between voxels m-1 and m)
   for (int f = slot; f < TF; f += NS) {
     const int m = s0 - 2 + f;
-    const Face fc = make_face_e<EMU>(ld(m), ld(m - 1), a.inv);
+    const Face fc = (EMU >= 2 && (MUL & 1)) ? make_face_i(ld(m), ld(m - 1), a.inv)
+                                            : make_face_e<EMU>(ld(m), ld(m - 1), a.inv);
     sf[0][f][line] = fc.v;
     sf[1][f][line] = fc.w;
     sf[2][f][line] = fc.t3;
@@ -489,14 +511,14 @@ __global__ void __launch_bounds__(G::NT, 5) k_weno_tile(AxisArgs a) {
   const double pp2_ = (-F(6, t + 4) + F(7, t + 3)) + F(3, t + 2);
   const double pp3_ = (F(3, t + 3) + F(7, t + 2)) - F(6, t + 1);
   const double plus =
-      weno_weights<EMU, true>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line], sc[2][t + 1][line],
+      weno_weights<EMU, true, EMU >= 2 && (MUL & 2)>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line], sc[2][t + 1][line],
                               se[t + 1][line]);
   // minus: v1..v5 = faces i-2, i-1, i, i+1, i+2 (tile faces t .. t+4)
   const double pm1_ = (F(3, t) - F(4, t + 1)) + F(5, t + 2);
   const double pm2_ = (-F(6, t + 1) + F(7, t + 2)) + F(3, t + 3);
   const double pm3_ = (F(3, t + 2) + F(7, t + 3)) - F(6, t + 4);
   const double minus =
-      weno_weights<EMU, true>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line],
+      weno_weights<EMU, true, EMU >= 2 && (MUL & 2)>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line],
                               se[t][line]);
   const int64_t o = base + (int64_t)i * stride;
   a.dplus[o] = plus;
@@ -701,19 +723,41 @@ int default_seg_len(int var, int64_t lines, int along) {
   return var ? seg_len_for(lines, along, 16, along / 64) : seg_len_for(lines, along, 8, (along + SEG - 1) / SEG);
 }
 
-template <int EMU, typename G>
-void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
+template <int EMU, typename G, int MUL>
+void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
   const dim3 gt((lanes + G::L - 1) / G::L, other, (along + G::P - 1) / G::P);
   static bool done[3] = {false, false, false};
   if (ax == 0) {
-    tile_smem_attr(k_weno_tile<0, EMU, G>, done[0]);
-    k_weno_tile<0, EMU, G><<<gt, G::NT, G::BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<0, EMU, G, MUL>, done[0]);
+    k_weno_tile<0, EMU, G, MUL><<<gt, G::NT, G::BYTES, s>>>(a);
   } else if (ax == 1) {
-    tile_smem_attr(k_weno_tile<1, EMU, G>, done[1]);
-    k_weno_tile<1, EMU, G><<<gt, G::NT, G::BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<1, EMU, G, MUL>, done[1]);
+    k_weno_tile<1, EMU, G, MUL><<<gt, G::NT, G::BYTES, s>>>(a);
   } else {
-    tile_smem_attr(k_weno_tile<2, EMU, G>, done[2]);
-    k_weno_tile<2, EMU, G><<<gt, G::NT, G::BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<2, EMU, G, MUL>, done[2]);
+    k_weno_tile<2, EMU, G, MUL><<<gt, G::NT, G::BYTES, s>>>(a);
+  }
+}
+
+// $QSSGPU_TILE_MUL (0..3, default 0): which further products of the tile
+// form run on the integer pipes (bit 0 the faces' squares and 3v, bit 1 the
+// final weighted sum); identical results
+int tile_mul() {
+  static const int m = [] {
+    const char* e = getenv("QSSGPU_TILE_MUL");
+    const int v = e ? atoi(e) : 0;
+    return v < 0 ? 0 : (v > 3 ? 3 : v);
+  }();
+  return m;
+}
+
+template <int EMU, typename G>
+void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
+  switch (EMU >= 2 ? tile_mul() : 0) {
+    case 1: launch_tile_m<EMU, G, 1>(s, ax, a, lanes, other, along); break;
+    case 2: launch_tile_m<EMU, G, 2>(s, ax, a, lanes, other, along); break;
+    case 3: launch_tile_m<EMU, G, 3>(s, ax, a, lanes, other, along); break;
+    default: launch_tile_m<EMU, G, 0>(s, ax, a, lanes, other, along); break;
   }
 }
 
