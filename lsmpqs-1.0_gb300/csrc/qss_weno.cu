@@ -739,13 +739,15 @@ void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int oth
   }
 }
 
-// $QSSGPU_TILE_MUL (0..3, default 0): which further products of the tile
+// $QSSGPU_TILE_MUL (0..3, default 2): which further products of the tile
 // form run on the integer pipes (bit 0 the faces' squares and 3v, bit 1 the
-// final weighted sum); identical results
+// final weighted sum); identical results.  GB300, whole WENO5 stage, M
+// voxel-steps/s at 512^3 / 192^3: 0: 553.7 / 522.1, 1: 555.6 / 522.0,
+// 2: 558.5 / 524.5, 3: 552.7 / 519.2.
 int tile_mul() {
   static const int m = [] {
     const char* e = getenv("QSSGPU_TILE_MUL");
-    const int v = e ? atoi(e) : 0;
+    const int v = e ? atoi(e) : 2;
     return v < 0 ? 0 : (v > 3 ? 3 : v);
   }();
   return m;
