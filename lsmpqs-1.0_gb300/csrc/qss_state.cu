@@ -417,16 +417,6 @@ void start_prefault(DevVolume& v, const QSS_DataArrays* p, std::initializer_list
   v.prefault.start(ranges);
 }
 
-// $QSSGPU_HOST_ZERO=1: the arrays the reference leaves zero are cleared by
-// host threads instead of copied from a zeroed device buffer
-static bool host_zero() {
-  static const int on = [] {
-    const char* e = getenv("QSSGPU_HOST_ZERO");
-    return e && atoi(e) == 1 ? 1 : 0;
-  }();
-  return on != 0;
-}
-
 void download_dirty(DevVolume& v, QSS_DataArrays* p) {
   PhaseTimer pt(v, PH_DOWNLOAD);
   v.prefault.join();
@@ -442,7 +432,6 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
   // reinitialisation scratch, free once the call's work is queued) by the
   // copy engine, which writes host memory faster than a CPU memset
   bool zeroed = false;
-  std::vector<std::pair<void*, size_t>> host_clear;
   for (int a = 0; a < H_COUNT; a++) {
     HostArray w = (HostArray)a;
     void* h = host_ptr(p, w);
@@ -450,10 +439,7 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
       v.dirty[a] = v.zero_on_return[a] = false;
       continue;
     }
-    if (v.zero_on_return[a] && host_zero()) {
-      // cleared by host threads while the copy engines move the other arrays
-      host_clear.emplace_back(h, (size_t)v.n * elem_size(w));
-    } else if (v.zero_on_return[a]) {
+    if (v.zero_on_return[a]) {
       const size_t bytes = (size_t)v.n * elem_size(w);  // at most n doubles
       if (!zeroed) {
         // cleared on the volume's stream, then made visible to the other two
@@ -487,19 +473,6 @@ void download_dirty(DevVolume& v, QSS_DataArrays* p) {
   for (int x = 0; x < 2; x++) {
     QSS_CK(cudaEventRecord(v.xfer_ev[1 + x], v.xfer[x]));
     QSS_CK(cudaStreamWaitEvent(v.stream, v.xfer_ev[1 + x], 0));
-  }
-  if (!host_clear.empty()) {
-    // 8 threads, each a contiguous share of every array to clear
-    constexpr int kThreads = 8;
-    std::vector<std::thread> th;
-    for (int t = 0; t < kThreads; t++)
-      th.emplace_back([&host_clear, t] {
-        for (const auto& r : host_clear) {
-          const size_t lo = r.second * t / kThreads, hi = r.second * (t + 1) / kThreads;
-          memset((char*)r.first + lo, 0, hi - lo);
-        }
-      });
-    for (auto& x : th) x.join();
   }
   QSS_CK(cudaStreamSynchronize(v.stream));
 }
