@@ -242,7 +242,7 @@ struct AdjAxisArgs {
   int nseg;
 };
 
-template <int AX, bool MULS>
+template <int AX>
 __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
   const Box& b = a.b;
   int p, q, lo, hi;
@@ -356,10 +356,8 @@ __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
       const double Q1 = mul(gp, wp1), Q2 = mul(gp, wp2), Q3 = mul(gp, wp3);
       const double x1 = qss_emu::scale2(r1, 1), x2 = qss_emu::scale2(r2, 1), x3 = qss_emu::scale2(r3, 1);
       // x_k = 2 r_k; the minus sign of d value / d T_k is folded into the differences
-      // these twelve products on the integer pipes as well when MULS
-      auto pr = [](double u, double v) { return MULS ? mul(u, v) : u * v; };
-      const double m1 = pr(pr(P1, vm - pm1), x1), m2 = pr(pr(P2, vm - pm2), x2), m3 = pr(pr(P3, vm - pm3), x3);
-      const double n1 = pr(pr(Q1, vp - pq1), x1), n2 = pr(pr(Q2, vp - pq2), x2), n3 = pr(pr(Q3, vp - pq3), x3);
+      const double m1 = P1 * (vm - pm1) * x1, m2 = P2 * (vm - pm2) * x2, m3 = P3 * (vm - pm3) * x3;
+      const double n1 = Q1 * (vp - pq1) * x1, n2 = Q2 * (vp - pq2) * x2, n3 = Q3 * (vp - pq3) * x3;
       const double bS1 = m1 + n1, bS2 = m2 + n2, bS3 = m3 + n3;
       const double bem = m1 + m2 + m3, bep = n1 + n2 + n3;
       BAm += bS1;
@@ -601,16 +599,6 @@ __global__ void k_scale_fill(Box b, const double* __restrict__ lam, double coef,
     const bool fill = i >= b.ilo && i <= b.ihi && j >= b.jlo && j <= b.jhi && k >= b.klo && k <= b.khi;
     wgt[p] = fill ? coef * lam[p] : 0.0;
   }
-}
-
-// $QSSGPU_ADJ_MUL=1: twelve more products of the reverse WENO5 window on the
-// integer pipes (k_adj_axis)
-bool adj_muls() {
-  static const int on = [] {
-    const char* e = getenv("QSSGPU_ADJ_MUL");
-    return e && atoi(e) == 1 ? 1 : 0;
-  }();
-  return on != 0;
 }
 
 unsigned g1(int64_t n) {
@@ -916,20 +904,17 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
       ax.bm = ar.bm[0];
       ax.inv = 1.0 / g->dx[0];
       ax.nseg = ns0;
-      if (adj_muls()) k_adj_axis<0, true><<<ag0, 128, 0, a.s>>>(ax);
-      else k_adj_axis<0, false><<<ag0, 128, 0, a.s>>>(ax);
+      k_adj_axis<0><<<ag0, 128, 0, a.s>>>(ax);
       ax.bp = ar.bp[1];
       ax.bm = ar.bm[1];
       ax.inv = 1.0 / g->dx[1];
       ax.nseg = ns1;
-      if (adj_muls()) k_adj_axis<1, true><<<ag1, 128, 0, a.s>>>(ax);
-      else k_adj_axis<1, false><<<ag1, 128, 0, a.s>>>(ax);
+      k_adj_axis<1><<<ag1, 128, 0, a.s>>>(ax);
       ax.bp = ar.bp[2];
       ax.bm = ar.bm[2];
       ax.inv = 1.0 / g->dx[2];
       ax.nseg = ns2;
-      if (adj_muls()) k_adj_axis<2, true><<<ag2, 128, 0, a.s>>>(ax);
-      else k_adj_axis<2, false><<<ag2, 128, 0, a.s>>>(ax);
+      k_adj_axis<2><<<ag2, 128, 0, a.s>>>(ax);
       k_adj_curv<<<g1(n), 256, 0, a.s>>>(b, cc, n, lam_in, coef_id, lam_out);
     };
     // recomputation of segment k's states from its checkpoint, on stream st
