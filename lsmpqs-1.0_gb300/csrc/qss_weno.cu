@@ -13,9 +13,12 @@
 // GB300 (one FP64 warp instruction per ~64 cycles per scheduler).
 //
 // A stage runs as three axis passes and one combine kernel:
-//   k_weno_axis<AX>: each thread walks a segment of SEG voxels along axis AX
-//     with a sliding window of faces / centres and writes the plus and minus
-//     one-sided derivatives of that axis (2 doubles per voxel);
+//   k_weno_tile<AX> (the default): a block computes every face and centre of
+//     a tile of lines once into shared memory, then one thread per voxel the
+//     two reconstructions, and writes the plus and minus one-sided
+//     derivatives of that axis (2 doubles per voxel);
+//   k_weno_axis<AX> (selectable): each thread walks a segment of voxels along
+//     axis AX with a sliding window of faces / centres, same outputs;
 //   k_weno_combine: Godunov normal term (with the carried term of voxels whose
 //     speed is below 1e-5), upwind advection, central curvature, TVD-RK
 //     combination and, on the last stage, the three mask impositions.
@@ -389,9 +392,10 @@ __global__ void __launch_bounds__(128, RING ? 5 : 4) k_weno_axis(AxisArgs a) {
 // A tile shape: L lines (a power of two) x P voxels along the axis, handled
 // by L * NS threads; thread t works on line t % L and position slot t / L,
 // taking positions slot, slot + NS, ... in each phase.
-template <int L_, int P_, int NS_>
+template <int L_, int P_, int NS_, int MB_>
 struct TileGeom {
   static constexpr int L = L_, P = P_, NS = NS_;
+  static constexpr int MB = MB_;  // resident blocks per SM the kernel is compiled for
   static constexpr int F = P + 5;  // faces s0-2 .. s0+P+2
   static constexpr int C = P + 3;  // centres s0-1 .. s0+P+1
   static constexpr int E = P + 1;  // eps+ of voxels s0-1 .. s0+P-1
@@ -400,15 +404,18 @@ struct TileGeom {
 };
 // 16 lines x 16 voxels, 256 threads (faces and centres of the halo take a
 // second round for 5 and 3 slots)
-using Tile16 = TileGeom<16, 16, 16>;
+using Tile16 = TileGeom<16, 16, 16, 5>;
 // 8 lines x 27 voxels, 32 slots, 256 threads: the 32 faces take one round,
 // the 30 centres one (2 slots idle), the 27 voxels one (5 slots idle); lines
-// of a multiple of 27 voxels lose nothing to the last tile
-using Tile27 = TileGeom<8, 27, 32>;
+// of a multiple of 27 voxels lose nothing to the last tile; compiled for 6
+// blocks per SM (40 registers): 565 against 553 M voxel-steps/s for the whole
+// stage at 512^3 on GB300 (16 x 16 tiles lose with 6 blocks: 518 against 522
+// M at 192^3)
+using Tile27 = TileGeom<8, 27, 32, 6>;
 
 // the tile kernels ask for all of the unified L1 / shared memory as shared
-// memory, so that five blocks of a tile fit on an SM (once per process
-// and kernel)
+// memory, so that five or six blocks of a tile fit on an SM (once per
+// process and kernel)
 template <typename K>
 void tile_smem_attr(K kernel, bool& done) {
   if (done) return;
@@ -418,8 +425,8 @@ void tile_smem_attr(K kernel, bool& done) {
 
 // MUL bit 0: the faces' squares and 3v on the integer pipes; bit 1: the
 // weights' products with the candidate stencils as well (EMU 2 only)
-template <int AX, int EMU, typename G, int MUL = 0, int MB = 5>
-__global__ void __launch_bounds__(G::NT, MB) k_weno_tile(AxisArgs a) {
+template <int AX, int EMU, typename G, int MUL = 0>
+__global__ void __launch_bounds__(G::NT, G::MB) k_weno_tile(AxisArgs a) {
   if (a.ctl && !a.ctl->active) return;
   constexpr int TL = G::L, TP = G::P, NS = G::NS, TF = G::F, TC = G::C, TE = G::E;
   const Box& b = a.b;
@@ -625,8 +632,10 @@ __device__ __forceinline__ double impose3_e(double v, int64_t idx, const ImposeA
 // One block: 32 (i) x 4 (j) voxels of one k plane; each warp covers an 8 x 4
 // patch of them, so that the warps that lie wholly where the curvature
 // coefficient is zero (inside the grains) skip the curvature term together.
-template <int STAGE, bool FINAL, int EMU, int MB = 1>
-__global__ void __launch_bounds__(128, MB) k_weno_combine(CombineArgs a) {
+// Compiled for 10 resident blocks per SM (48 registers; 64 without the bound):
+// 557 against 553 M voxel-steps/s for the whole stage at 512^3 on GB300.
+template <int STAGE, bool FINAL, int EMU>
+__global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   if (STAGE != 0 && !a.ctl->active) return;
   using Q = Ar<EMU>;
   const Box& b = a.b;
@@ -723,36 +732,20 @@ int default_seg_len(int var, int64_t lines, int along) {
   return var ? seg_len_for(lines, along, 16, along / 64) : seg_len_for(lines, along, 8, (along + SEG - 1) / SEG);
 }
 
-template <int EMU, typename G, int MUL, int MB>
-void launch_tile_mb(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
+template <int EMU, typename G, int MUL>
+void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
   const dim3 gt((lanes + G::L - 1) / G::L, other, (along + G::P - 1) / G::P);
   static bool done[3] = {false, false, false};
   if (ax == 0) {
-    tile_smem_attr(k_weno_tile<0, EMU, G, MUL, MB>, done[0]);
-    k_weno_tile<0, EMU, G, MUL, MB><<<gt, G::NT, G::BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<0, EMU, G, MUL>, done[0]);
+    k_weno_tile<0, EMU, G, MUL><<<gt, G::NT, G::BYTES, s>>>(a);
   } else if (ax == 1) {
-    tile_smem_attr(k_weno_tile<1, EMU, G, MUL, MB>, done[1]);
-    k_weno_tile<1, EMU, G, MUL, MB><<<gt, G::NT, G::BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<1, EMU, G, MUL>, done[1]);
+    k_weno_tile<1, EMU, G, MUL><<<gt, G::NT, G::BYTES, s>>>(a);
   } else {
-    tile_smem_attr(k_weno_tile<2, EMU, G, MUL, MB>, done[2]);
-    k_weno_tile<2, EMU, G, MUL, MB><<<gt, G::NT, G::BYTES, s>>>(a);
+    tile_smem_attr(k_weno_tile<2, EMU, G, MUL>, done[2]);
+    k_weno_tile<2, EMU, G, MUL><<<gt, G::NT, G::BYTES, s>>>(a);
   }
-}
-
-// $QSSGPU_TILE_MB=6: the tile kernels compiled for 6 resident blocks per SM
-// (40 registers) instead of 5 (48)
-int tile_mb() {
-  static const int m = [] {
-    const char* e = getenv("QSSGPU_TILE_MB");
-    return e && atoi(e) == 6 ? 6 : 5;
-  }();
-  return m;
-}
-
-template <int EMU, typename G, int MUL>
-void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
-  if (tile_mb() == 6) launch_tile_mb<EMU, G, MUL, 6>(s, ax, a, lanes, other, along);
-  else launch_tile_mb<EMU, G, MUL, 5>(s, ax, a, lanes, other, along);
 }
 
 // $QSSGPU_TILE_MUL (0..3, default 2): which further products of the tile
@@ -910,30 +903,14 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
   }
 }
 
-// $QSSGPU_COMBINE_MB: minimum resident blocks per SM the combine kernel is
-// compiled for (1: no bound, 64 registers; 10: 48 registers)
-int combine_mb() {
-  static const int m = [] {
-    const char* e = getenv("QSSGPU_COMBINE_MB");
-    return e && atoi(e) == 10 ? 10 : 1;
-  }();
-  return m;
-}
-
-template <int EMU, int MB>
-void combine_at_mb(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
-  switch (stage) {
-    case 0: k_weno_combine<0, false, EMU, MB><<<g, blk, 0, s>>>(a); break;
-    case 1: if (final_stage) k_weno_combine<1, true, EMU, MB><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU, MB><<<g, blk, 0, s>>>(a); break;
-    case 2: if (final_stage) k_weno_combine<2, true, EMU, MB><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU, MB><<<g, blk, 0, s>>>(a); break;
-    default: if (final_stage) k_weno_combine<3, true, EMU, MB><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU, MB><<<g, blk, 0, s>>>(a); break;
-  }
-}
-
 template <int EMU>
 void combine_at(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
-  if (combine_mb() == 10) combine_at_mb<EMU, 10>(s, stage, final_stage, g, blk, a);
-  else combine_at_mb<EMU, 1>(s, stage, final_stage, g, blk, a);
+  switch (stage) {
+    case 0: k_weno_combine<0, false, EMU><<<g, blk, 0, s>>>(a); break;
+    case 1: if (final_stage) k_weno_combine<1, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU><<<g, blk, 0, s>>>(a); break;
+    case 2: if (final_stage) k_weno_combine<2, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU><<<g, blk, 0, s>>>(a); break;
+    default: if (final_stage) k_weno_combine<3, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU><<<g, blk, 0, s>>>(a); break;
+  }
 }
 
 }  // namespace
