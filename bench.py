@@ -209,19 +209,27 @@ FLOP_PER_VOXEL = {0: 3 * (16 + 2 * 75) + 10 + 5 + 72 + 2 + 5,
                   1: 9 + 35 + 2 + 2 * 26, 2: 9 + 35 + 2 + 2 * 26, 3: 9 + 35 + 2 + 2 * 26,
                   4: 10 + 5 + 72 + 2 + 5}
 KERNEL_NAME = {0: "k_stage<WENO5,var> (fused RHS + TVD-RK stage)",
-               1: "k_weno_tile<0> (WENO5 x-pass, 16 x 16 tiles, shared sub-expressions)",
-               2: "k_weno_tile<1> (WENO5 y-pass, 16 x 16 tiles, shared sub-expressions)",
-               3: "k_weno_tile<2> (WENO5 z-pass, 16 x 16 tiles, shared sub-expressions)",
+               1: "k_weno_tile<0> (WENO5 x-pass, {} tiles, shared sub-expressions)",
+               2: "k_weno_tile<1> (WENO5 y-pass, {} tiles, shared sub-expressions)",
+               3: "k_weno_tile<2> (WENO5 z-pass, {} tiles, shared sub-expressions)",
                4: "k_weno_combine (Godunov + advection + curvature + TVD-RK)"}
 # the window forms (--axis-variant 0/1/2) run k_weno_axis<axis> instead
 WINDOW_NAME = {1: "k_weno_axis<0> (WENO5 x-pass, sliding window)",
                2: "k_weno_axis<1> (WENO5 y-pass, sliding window)",
                3: "k_weno_axis<2> (WENO5 z-pass, sliding window)"}
 # FP64-pipe instructions (DADD + DMUL) per fill-box voxel of one tile-form axis
-# pass, ncu at 192^3 (smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum
-# over 7.08 M voxels: 50.9 + 11.1); the rest of the 98 algorithmic operations
-# (divisions, squares, scalings, maxima, scaled copies) run on the integer pipes
-FP64_INSTR_PER_VOXEL_TILE = 62.0
+# pass by tile geometry, from ncu (smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum
+# of one launch over its voxels; 16 x 16 at 192^3, 8 x 27 at 216^3); the rest
+# of the 98 algorithmic operations (divisions, squares, scalings, maxima,
+# scaled copies, the weights' products) run on the integer pipes
+FP64_INSTR_PER_VOXEL_TILE = {"16 x 16": 62.0, "8 x 27": 62.0}
+
+
+def tile_geometry(line: int) -> str:
+    """The library's default tile for a line of `line` voxels: 8 x 27 where the
+    last 27-voxel tile is at most 2 % idle, else 16 x 16."""
+    tiles = -(-line // 27)
+    return "8 x 27" if tiles * 27 * 50 <= line * 51 else "16 x 16"
 N_KINDS = 5
 # DRAM bytes per fill-box voxel of one launch of each stage kernel, measured at
 # 512^3 with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass):
@@ -268,9 +276,10 @@ def gpu_arm(args, dist: Dist):
     top = int(out[4])
     top_ms = out[1]
     window = args.axis_variant in (0, 1, 2)
+    geom = {None: tile_geometry(n), 3: "16 x 16", 4: "8 x 27"}.get(args.axis_variant)
 
     def kname(k):
-        return (WINDOW_NAME if window and k in WINDOW_NAME else KERNEL_NAME)[k]
+        return (WINDOW_NAME if window and k in WINDOW_NAME else KERNEL_NAME)[k].format(geom)
 
     kinds = {kname(k).split(" ")[0]: {"ms_total": round(out[5 + k], 3),
                                             "launches": int(out[5 + N_KINDS + k]),
@@ -337,8 +346,9 @@ def gpu_arm(args, dist: Dist):
         traffic_unit = "bytes per launch (ncu at 512^3, scaled per voxel to this size)"
     fp64_pipe = None
     if tile and top_ms > 0:
-        instr = FP64_INSTR_PER_VOXEL_TILE * nvox / (top_ms / 1e3) / 1e12
-        fp64_pipe = {"instructions_per_voxel": FP64_INSTR_PER_VOXEL_TILE, "achieved": round(instr, 4),
+        per_voxel = FP64_INSTR_PER_VOXEL_TILE[geom]
+        instr = per_voxel * nvox / (top_ms / 1e3) / 1e12
+        fp64_pipe = {"instructions_per_voxel": per_voxel, "tile": geom, "achieved": round(instr, 4),
                      "peak": fp64_peak, "unit": "T instructions/s", "frac": round(instr / fp64_peak, 4),
                      "ncu_busy_pct_192": 75.7,
                      "note": "FP64-pipe instructions (DADD + DMUL, ncu count per voxel) over the launch time, "
