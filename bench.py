@@ -219,10 +219,13 @@ WINDOW_NAME = {1: "k_weno_axis<0> (WENO5 x-pass, sliding window)",
                3: "k_weno_axis<2> (WENO5 z-pass, sliding window)"}
 # FP64-pipe instructions (DADD + DMUL) per fill-box voxel of one tile-form axis
 # pass by tile geometry, from ncu (smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum
-# of one launch over its voxels; 16 x 16 at 192^3, 8 x 27 at 216^3); the rest
-# of the 98 algorithmic operations (divisions, squares, scalings, maxima,
-# scaled copies, the weights' products) run on the integer pipes
-FP64_INSTR_PER_VOXEL_TILE = {"16 x 16": 62.0, "8 x 27": 62.0}
+# of one launch over its voxels; 16 x 16 at 192^3: 50.94 + 5.07, 8 x 27 at
+# 216^3: 49.33 + 4.66); the rest of the 98 algorithmic operations (divisions,
+# squares, scalings, maxima, scaled copies, the weights' products) run on the
+# integer pipes.  FP64_PIPE_BUSY_TILE: sm__inst_executed_pipe_fp64 (pct of
+# peak, active) of the same launches.
+FP64_INSTR_PER_VOXEL_TILE = {"16 x 16": 56.0, "8 x 27": 54.0}
+FP64_PIPE_BUSY_TILE = {"16 x 16": ("192^3", 72.8), "8 x 27": ("216^3", 76.0)}
 
 
 def tile_geometry(line: int) -> str:
@@ -350,10 +353,10 @@ def gpu_arm(args, dist: Dist):
         instr = per_voxel * nvox / (top_ms / 1e3) / 1e12
         fp64_pipe = {"instructions_per_voxel": per_voxel, "tile": geom, "achieved": round(instr, 4),
                      "peak": fp64_peak, "unit": "T instructions/s", "frac": round(instr / fp64_peak, 4),
-                     "ncu_busy_pct_192": 75.7,
+                     "ncu_busy_pct": FP64_PIPE_BUSY_TILE[geom][1], "ncu_case": FP64_PIPE_BUSY_TILE[geom][0],
                      "note": "FP64-pipe instructions (DADD + DMUL, ncu count per voxel) over the launch time, "
-                             "against the non-FMA issue rate; ncu_busy_pct_192 is sm__inst_executed_pipe_fp64 "
-                             "(pct of peak) of the same kernel at 192^3"}
+                             "against the non-FMA issue rate; ncu_busy_pct is sm__inst_executed_pipe_fp64 "
+                             "(pct of peak) of the same kernel in the ncu_case capture"}
     # HBM: the step's algorithmic bytes over the time of all its stage kernels
     stage_total_ms = out[3] / args.steps
     achieved_gbs = BYTES_PER_VOXEL_STEP * nvox / (stage_total_ms / 1e3) / 1e9 if stage_total_ms > 0 else 0.0
