@@ -178,24 +178,32 @@ __device__ __forceinline__ double eps_of(double w1, double w2, double w3, double
 
 // weights and combination of one side (3d.f:1996-2005) given the candidate
 // stencils and smoothness indicators
-template <int EMU, bool SQ, bool MULC = false>
+// out-of-line copies of integer-pipe routines: one copy of the code instead of
+// one per call site keeps the kernels' instruction footprint small
+__device__ __noinline__ double div_outline(double a, double b) { return qss_emu::div(a, b); }
+__device__ __noinline__ double mul_outline(double a, double b) { return qss_emu::mul(a, b); }
+__device__ __noinline__ double sqrt_outline(double a) { return qss_emu::sqrt(a); }
+
+template <int EMU, bool SQ, bool MULC = false, bool OUTLINE = false, bool OUTMUL = false>
 __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, double S1, double S2, double S3,
                                                double eps) {
   using Q = Ar<EMU>;
-  auto sq = [](double t) { return SQ ? Q::mul2(t, t) : t * t; };
+  auto m2 = [](double x, double y) { return (OUTMUL && EMU >= 2) ? mul_outline(x, y) : Q::mul2(x, y); };
+  auto sq = [&](double t) { return SQ ? m2(t, t) : t * t; };
+  auto dv = [](double x, double y) { return (OUTLINE && EMU >= 1) ? div_outline(x, y) : Q::div(x, y); };
   double t, a1, a2, a3;
   t = S1 + eps;
-  a1 = Q::div(0.1, sq(t));
+  a1 = dv(0.1, sq(t));
   t = S2 + eps;
-  a2 = Q::div(0.6, sq(t));
+  a2 = dv(0.6, sq(t));
   t = S3 + eps;
-  a3 = Q::div(0.3, sq(t));
-  const double inv_sum_a = Q::div(1.0, a1 + a2 + a3);
-  a1 = Q::mul2(a1, inv_sum_a);
-  a2 = Q::mul2(a2, inv_sum_a);
-  a3 = Q::mul2(a3, inv_sum_a);
+  a3 = dv(0.3, sq(t));
+  const double inv_sum_a = dv(1.0, a1 + a2 + a3);
+  a1 = m2(a1, inv_sum_a);
+  a2 = m2(a2, inv_sum_a);
+  a3 = m2(a3, inv_sum_a);
   // the combination's products on the integer pipes too when MULC
-  if (MULC) return Q::mul2(a1, p1) + Q::mul2(a2, p2) + Q::mul2(a3, p3);
+  if (MULC) return m2(a1, p1) + m2(a2, p2) + m2(a3, p3);
   return a1 * p1 + a2 * p2 + a3 * p3;
 }
 
@@ -518,14 +526,14 @@ __global__ void __launch_bounds__(G::NT, G::MB) k_weno_tile(AxisArgs a) {
   const double pp2_ = (-F(6, t + 4) + F(7, t + 3)) + F(3, t + 2);
   const double pp3_ = (F(3, t + 3) + F(7, t + 2)) - F(6, t + 1);
   const double plus =
-      weno_weights<EMU, true, EMU >= 2 && (MUL & 2)>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line], sc[2][t + 1][line],
+      weno_weights<EMU, true, EMU >= 2 && (MUL & 2), (MUL & 4) != 0, (MUL & 8) != 0>(pp1_, pp2_, pp3_, sc[0][t + 3][line], sc[1][t + 2][line], sc[2][t + 1][line],
                               se[t + 1][line]);
   // minus: v1..v5 = faces i-2, i-1, i, i+1, i+2 (tile faces t .. t+4)
   const double pm1_ = (F(3, t) - F(4, t + 1)) + F(5, t + 2);
   const double pm2_ = (-F(6, t + 1) + F(7, t + 2)) + F(3, t + 3);
   const double pm3_ = (F(3, t + 2) + F(7, t + 3)) - F(6, t + 4);
   const double minus =
-      weno_weights<EMU, true, EMU >= 2 && (MUL & 2)>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line],
+      weno_weights<EMU, true, EMU >= 2 && (MUL & 2), (MUL & 4) != 0, (MUL & 8) != 0>(pm1_, pm2_, pm3_, sc[3][t][line], sc[4][t + 1][line], sc[5][t + 2][line],
                               se[t][line]);
   const int64_t o = base + (int64_t)i * stride;
   a.dplus[o] = plus;
@@ -548,7 +556,7 @@ struct CombineArgs {
 
 // Godunov normal term of the WENO5 scheme, vel * |grad| (3d.f:2251-2276),
 // with the sign tests and maxima on the integer pipes at EMU >= 1
-template <int EMU>
+template <int EMU, bool OUT = false>
 __device__ __forceinline__ double godunov5(double vel, const double pp[3], const double pm[3]) {
   if (EMU == 0) return godunov_norm<WENO5>(vel, pp, pm);
   using namespace qss_emu;
@@ -570,7 +578,7 @@ __device__ __forceinline__ double godunov5(double vel, const double pp[3], const
     }
     ngps = s[0] + s[1] + s[2];
   }
-  return vel * qss_emu::sqrt(ngps);
+  return vel * (OUT ? sqrt_outline(ngps) : qss_emu::sqrt(ngps));
 }
 
 // |v| >= 1e-5 (false for NaN)
@@ -582,7 +590,7 @@ __device__ __forceinline__ bool speed_valid(double v) {
 // central curvature term (3d.f:2337-2379), same operations as curvature()
 // with the exact doublings, the threshold test and the division moved to the
 // integer pipes at EMU >= 1
-template <int EMU>
+template <int EMU, bool OUT = false>
 __device__ __forceinline__ double curvature_e(const double* __restrict__ phi, const Box& b, int64_t c, const Fac& f) {
   if (EMU == 0) return curvature(phi, b, c, f);
   using Q = Ar<EMU>;
@@ -611,7 +619,7 @@ __device__ __forceinline__ double curvature_e(const double* __restrict__ phi, co
                       Q::mul2(Q::mul2(phi_zz, phi_x), phi_x) - Q::mul2(Q::mul2(Q::s2(phi_xz, 1), phi_x), phi_z) +
                       Q::mul2(Q::mul2(phi_yy, phi_z), phi_z) + Q::mul2(Q::mul2(phi_zz, phi_y), phi_y) -
                       Q::mul2(Q::mul2(Q::s2(phi_yz, 1), phi_y), phi_z);
-  return Q::div(curv, grad_mag2);
+  return OUT ? div_outline(curv, grad_mag2) : Q::div(curv, grad_mag2);
 }
 
 // the three mask impositions with the comparisons on the integer pipes
@@ -634,7 +642,7 @@ __device__ __forceinline__ double impose3_e(double v, int64_t idx, const ImposeA
 // coefficient is zero (inside the grains) skip the curvature term together.
 // Compiled for 10 resident blocks per SM (48 registers; 64 without the bound):
 // 557 against 553 M voxel-steps/s for the whole stage at 512^3 on GB300.
-template <int STAGE, bool FINAL, int EMU>
+template <int STAGE, bool FINAL, int EMU, bool OUT = false>
 __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   if (STAGE != 0 && !a.ctl->active) return;
   using Q = Ar<EMU>;
@@ -654,7 +662,7 @@ __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   const double vel = a.c.vel_n[idx];
   double temp_norm;
   if (EMU >= 1 ? speed_valid(vel) : fabs(vel) >= 1.e-5) {
-    temp_norm = godunov5<EMU>(vel, pp, pm);
+    temp_norm = godunov5<EMU, OUT>(vel, pp, pm);
   } else {
     const int src = a.c.nsrc[idx];
     if (src < 0) {
@@ -666,7 +674,7 @@ __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
         qp[d] = a.dp[d][src];
         qm[d] = a.dm[d][src];
       }
-      temp_norm = godunov5<EMU>(a.c.vel_n[src], qp, qm);
+      temp_norm = godunov5<EMU, OUT>(a.c.vel_n[src], qp, qm);
     }
   }
   const double vx = a.c.vx[idx], vy = a.c.vy[idx], vz = a.c.vz[idx];
@@ -687,7 +695,7 @@ __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   const double bco = a.c.b[idx];
   const double temp_curv = (qss_emu::bits(bco) == 0 && qss_emu::bits(temp_norm) != qss_emu::kSign)
                                ? 0.0
-                               : bco * curvature_e<EMU>(a.phi_in, b, idx, a.fac);
+                               : bco * curvature_e<EMU, OUT>(a.phi_in, b, idx, a.fac);
   const double rhs = temp_norm + temp_curv + temp_vel;
   double out;
   if (STAGE == 0) {
@@ -756,8 +764,8 @@ void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int oth
 int tile_mul() {
   static const int m = [] {
     const char* e = getenv("QSSGPU_TILE_MUL");
-    const int v = e ? atoi(e) : 2;
-    return v < 0 ? 0 : (v > 3 ? 3 : v);
+    const int v = e ? atoi(e) : 6;
+    return v < 0 ? 0 : (v > 15 ? 15 : v);
   }();
   return m;
 }
@@ -765,10 +773,10 @@ int tile_mul() {
 template <int EMU, typename G>
 void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
   switch (EMU >= 2 ? tile_mul() : 0) {
-    case 1: launch_tile_m<EMU, G, 1>(s, ax, a, lanes, other, along); break;
+    case 0: launch_tile_m<EMU, G, 0>(s, ax, a, lanes, other, along); break;
     case 2: launch_tile_m<EMU, G, 2>(s, ax, a, lanes, other, along); break;
-    case 3: launch_tile_m<EMU, G, 3>(s, ax, a, lanes, other, along); break;
-    default: launch_tile_m<EMU, G, 0>(s, ax, a, lanes, other, along); break;
+    case 14: launch_tile_m<EMU, G, 14>(s, ax, a, lanes, other, along); break;
+    default: launch_tile_m<EMU, G, 6>(s, ax, a, lanes, other, along); break;
   }
 }
 
@@ -903,14 +911,30 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
   }
 }
 
+template <int EMU, bool OUT>
+void combine_at_o(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
+  switch (stage) {
+    case 0: k_weno_combine<0, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
+    case 1: if (final_stage) k_weno_combine<1, true, EMU, OUT><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
+    case 2: if (final_stage) k_weno_combine<2, true, EMU, OUT><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
+    default: if (final_stage) k_weno_combine<3, true, EMU, OUT><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
+  }
+}
+
+// $QSSGPU_COMBINE_OUTLINE=1: the combine kernel calls one out-of-line copy of
+// the integer-pipe square root and division
+bool combine_outline() {
+  static const int on = [] {
+    const char* e = getenv("QSSGPU_COMBINE_OUTLINE");
+    return e && atoi(e) == 1 ? 1 : 0;
+  }();
+  return on != 0;
+}
+
 template <int EMU>
 void combine_at(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
-  switch (stage) {
-    case 0: k_weno_combine<0, false, EMU><<<g, blk, 0, s>>>(a); break;
-    case 1: if (final_stage) k_weno_combine<1, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU><<<g, blk, 0, s>>>(a); break;
-    case 2: if (final_stage) k_weno_combine<2, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU><<<g, blk, 0, s>>>(a); break;
-    default: if (final_stage) k_weno_combine<3, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU><<<g, blk, 0, s>>>(a); break;
-  }
+  if (EMU >= 1 && combine_outline()) combine_at_o<EMU, true>(s, stage, final_stage, g, blk, a);
+  else combine_at_o<EMU, false>(s, stage, final_stage, g, blk, a);
 }
 
 }  // namespace
