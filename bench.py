@@ -223,7 +223,8 @@ WINDOW_NAME = {1: "k_weno_axis<0> (WENO5 x-pass, sliding window)",
 # 216^3: 49.33 + 4.66); the rest of the 98 algorithmic operations (divisions,
 # squares, scalings, maxima, scaled copies, the weights' products) run on the
 # integer pipes.  FP64_PIPE_BUSY_TILE: sm__inst_executed_pipe_fp64 (pct of
-# peak, active) of the same launches.
+# peak, active) of the same launches (a build before the out-of-line division
+# and product, which leave the FP64 instruction counts unchanged).
 FP64_INSTR_PER_VOXEL_TILE = {"16 x 16": 56.0, "8 x 27": 54.0}
 FP64_PIPE_BUSY_TILE = {"16 x 16": ("192^3", 72.8), "8 x 27": ("216^3", 76.0)}
 

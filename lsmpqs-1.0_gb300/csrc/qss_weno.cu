@@ -182,7 +182,6 @@ __device__ __forceinline__ double eps_of(double w1, double w2, double w3, double
 // one per call site keeps the kernels' instruction footprint small
 __device__ __noinline__ double div_outline(double a, double b) { return qss_emu::div(a, b); }
 __device__ __noinline__ double mul_outline(double a, double b) { return qss_emu::mul(a, b); }
-__device__ __noinline__ double sqrt_outline(double a) { return qss_emu::sqrt(a); }
 
 template <int EMU, bool SQ, bool MULC = false, bool OUTLINE = false, bool OUTMUL = false>
 __device__ __forceinline__ double weno_weights(double p1, double p2, double p3, double S1, double S2, double S3,
@@ -400,10 +399,11 @@ __global__ void __launch_bounds__(128, RING ? 5 : 4) k_weno_axis(AxisArgs a) {
 // A tile shape: L lines (a power of two) x P voxels along the axis, handled
 // by L * NS threads; thread t works on line t % L and position slot t / L,
 // taking positions slot, slot + NS, ... in each phase.
-template <int L_, int P_, int NS_, int MB_>
+template <int L_, int P_, int NS_, int MB_, int MUL_>
 struct TileGeom {
   static constexpr int L = L_, P = P_, NS = NS_;
-  static constexpr int MB = MB_;  // resident blocks per SM the kernel is compiled for
+  static constexpr int MB = MB_;    // resident blocks per SM the kernel is compiled for
+  static constexpr int MUL = MUL_;  // default integer-pipe / out-of-line arithmetic (tile_mul)
   static constexpr int F = P + 5;  // faces s0-2 .. s0+P+2
   static constexpr int C = P + 3;  // centres s0-1 .. s0+P+1
   static constexpr int E = P + 1;  // eps+ of voxels s0-1 .. s0+P-1
@@ -412,14 +412,14 @@ struct TileGeom {
 };
 // 16 lines x 16 voxels, 256 threads (faces and centres of the halo take a
 // second round for 5 and 3 slots)
-using Tile16 = TileGeom<16, 16, 16, 5>;
+using Tile16 = TileGeom<16, 16, 16, 5, 6>;
 // 8 lines x 27 voxels, 32 slots, 256 threads: the 32 faces take one round,
 // the 30 centres one (2 slots idle), the 27 voxels one (5 slots idle); lines
 // of a multiple of 27 voxels lose nothing to the last tile; compiled for 6
 // blocks per SM (40 registers): 565 against 553 M voxel-steps/s for the whole
 // stage at 512^3 on GB300 (16 x 16 tiles lose with 6 blocks: 518 against 522
 // M at 192^3)
-using Tile27 = TileGeom<8, 27, 32, 6>;
+using Tile27 = TileGeom<8, 27, 32, 6, 14>;
 
 // the tile kernels ask for all of the unified L1 / shared memory as shared
 // memory, so that five or six blocks of a tile fit on an SM (once per
@@ -556,7 +556,7 @@ struct CombineArgs {
 
 // Godunov normal term of the WENO5 scheme, vel * |grad| (3d.f:2251-2276),
 // with the sign tests and maxima on the integer pipes at EMU >= 1
-template <int EMU, bool OUT = false>
+template <int EMU>
 __device__ __forceinline__ double godunov5(double vel, const double pp[3], const double pm[3]) {
   if (EMU == 0) return godunov_norm<WENO5>(vel, pp, pm);
   using namespace qss_emu;
@@ -578,7 +578,7 @@ __device__ __forceinline__ double godunov5(double vel, const double pp[3], const
     }
     ngps = s[0] + s[1] + s[2];
   }
-  return vel * (OUT ? sqrt_outline(ngps) : qss_emu::sqrt(ngps));
+  return vel * qss_emu::sqrt(ngps);
 }
 
 // |v| >= 1e-5 (false for NaN)
@@ -590,7 +590,7 @@ __device__ __forceinline__ bool speed_valid(double v) {
 // central curvature term (3d.f:2337-2379), same operations as curvature()
 // with the exact doublings, the threshold test and the division moved to the
 // integer pipes at EMU >= 1
-template <int EMU, bool OUT = false>
+template <int EMU>
 __device__ __forceinline__ double curvature_e(const double* __restrict__ phi, const Box& b, int64_t c, const Fac& f) {
   if (EMU == 0) return curvature(phi, b, c, f);
   using Q = Ar<EMU>;
@@ -619,7 +619,7 @@ __device__ __forceinline__ double curvature_e(const double* __restrict__ phi, co
                       Q::mul2(Q::mul2(phi_zz, phi_x), phi_x) - Q::mul2(Q::mul2(Q::s2(phi_xz, 1), phi_x), phi_z) +
                       Q::mul2(Q::mul2(phi_yy, phi_z), phi_z) + Q::mul2(Q::mul2(phi_zz, phi_y), phi_y) -
                       Q::mul2(Q::mul2(Q::s2(phi_yz, 1), phi_y), phi_z);
-  return OUT ? div_outline(curv, grad_mag2) : Q::div(curv, grad_mag2);
+  return Q::div(curv, grad_mag2);
 }
 
 // the three mask impositions with the comparisons on the integer pipes
@@ -642,7 +642,7 @@ __device__ __forceinline__ double impose3_e(double v, int64_t idx, const ImposeA
 // coefficient is zero (inside the grains) skip the curvature term together.
 // Compiled for 10 resident blocks per SM (48 registers; 64 without the bound):
 // 557 against 553 M voxel-steps/s for the whole stage at 512^3 on GB300.
-template <int STAGE, bool FINAL, int EMU, bool OUT = false>
+template <int STAGE, bool FINAL, int EMU>
 __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   if (STAGE != 0 && !a.ctl->active) return;
   using Q = Ar<EMU>;
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   const double vel = a.c.vel_n[idx];
   double temp_norm;
   if (EMU >= 1 ? speed_valid(vel) : fabs(vel) >= 1.e-5) {
-    temp_norm = godunov5<EMU, OUT>(vel, pp, pm);
+    temp_norm = godunov5<EMU>(vel, pp, pm);
   } else {
     const int src = a.c.nsrc[idx];
     if (src < 0) {
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
         qp[d] = a.dp[d][src];
         qm[d] = a.dm[d][src];
       }
-      temp_norm = godunov5<EMU, OUT>(a.c.vel_n[src], qp, qm);
+      temp_norm = godunov5<EMU>(a.c.vel_n[src], qp, qm);
     }
   }
   const double vx = a.c.vx[idx], vy = a.c.vy[idx], vz = a.c.vz[idx];
@@ -695,7 +695,7 @@ __global__ void __launch_bounds__(128, 10) k_weno_combine(CombineArgs a) {
   const double bco = a.c.b[idx];
   const double temp_curv = (qss_emu::bits(bco) == 0 && qss_emu::bits(temp_norm) != qss_emu::kSign)
                                ? 0.0
-                               : bco * curvature_e<EMU, OUT>(a.phi_in, b, idx, a.fac);
+                               : bco * curvature_e<EMU>(a.phi_in, b, idx, a.fac);
   const double rhs = temp_norm + temp_curv + temp_vel;
   double out;
   if (STAGE == 0) {
@@ -756,27 +756,31 @@ void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int oth
   }
 }
 
-// $QSSGPU_TILE_MUL (0..3, default 2): which further products of the tile
-// form run on the integer pipes (bit 0 the faces' squares and 3v, bit 1 the
-// final weighted sum); identical results.  GB300, whole WENO5 stage, M
-// voxel-steps/s at 512^3 / 192^3: 0: 553.7 / 522.1, 1: 555.6 / 522.0,
-// 2: 558.5 / 524.5, 3: 552.7 / 519.2.
+// $QSSGPU_TILE_MUL (0, 2, 6 or 14; default per geometry, TileGeom::MUL):
+// bit 1 the weights' products with the candidate stencils on the integer
+// pipes, bit 2 one out-of-line copy of the integer-pipe division, bit 3 one
+// out-of-line copy of the integer-pipe product (in the weights); identical
+// results.  GB300, whole WENO5 stage, M voxel-steps/s at 512^3 (8 x 27
+// tiles) / 192^3 (16 x 16): 0: 553.7 / 522.1, 2: 558.5 / 524.5,
+// 6: 580.8 / 546.1, 14: 592.4 / 539.4 (bit 0, the faces' squares and 3v on
+// the integer pipes: no gain; an out-of-line square root and division in the
+// combine kernel: none either).
 int tile_mul() {
   static const int m = [] {
     const char* e = getenv("QSSGPU_TILE_MUL");
-    const int v = e ? atoi(e) : 6;
-    return v < 0 ? 0 : (v > 15 ? 15 : v);
+    const int v = e ? atoi(e) : -1;
+    return v == 0 || v == 2 || v == 6 || v == 14 ? v : -1;
   }();
   return m;
 }
 
 template <int EMU, typename G>
 void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other, int along) {
-  switch (EMU >= 2 ? tile_mul() : 0) {
+  switch (EMU >= 2 ? (tile_mul() >= 0 ? tile_mul() : G::MUL) : 0) {
     case 0: launch_tile_m<EMU, G, 0>(s, ax, a, lanes, other, along); break;
     case 2: launch_tile_m<EMU, G, 2>(s, ax, a, lanes, other, along); break;
-    case 14: launch_tile_m<EMU, G, 14>(s, ax, a, lanes, other, along); break;
-    default: launch_tile_m<EMU, G, 6>(s, ax, a, lanes, other, along); break;
+    case 6: launch_tile_m<EMU, G, 6>(s, ax, a, lanes, other, along); break;
+    default: launch_tile_m<EMU, G, 14>(s, ax, a, lanes, other, along); break;
   }
 }
 
@@ -911,30 +915,14 @@ void axes_at(cudaStream_t s, const Box& b, const double* phi, const double invs[
   }
 }
 
-template <int EMU, bool OUT>
-void combine_at_o(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
-  switch (stage) {
-    case 0: k_weno_combine<0, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
-    case 1: if (final_stage) k_weno_combine<1, true, EMU, OUT><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
-    case 2: if (final_stage) k_weno_combine<2, true, EMU, OUT><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
-    default: if (final_stage) k_weno_combine<3, true, EMU, OUT><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU, OUT><<<g, blk, 0, s>>>(a); break;
-  }
-}
-
-// $QSSGPU_COMBINE_OUTLINE=1: the combine kernel calls one out-of-line copy of
-// the integer-pipe square root and division
-bool combine_outline() {
-  static const int on = [] {
-    const char* e = getenv("QSSGPU_COMBINE_OUTLINE");
-    return e && atoi(e) == 1 ? 1 : 0;
-  }();
-  return on != 0;
-}
-
 template <int EMU>
 void combine_at(cudaStream_t s, int stage, bool final_stage, dim3 g, dim3 blk, const CombineArgs& a) {
-  if (EMU >= 1 && combine_outline()) combine_at_o<EMU, true>(s, stage, final_stage, g, blk, a);
-  else combine_at_o<EMU, false>(s, stage, final_stage, g, blk, a);
+  switch (stage) {
+    case 0: k_weno_combine<0, false, EMU><<<g, blk, 0, s>>>(a); break;
+    case 1: if (final_stage) k_weno_combine<1, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<1, false, EMU><<<g, blk, 0, s>>>(a); break;
+    case 2: if (final_stage) k_weno_combine<2, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<2, false, EMU><<<g, blk, 0, s>>>(a); break;
+    default: if (final_stage) k_weno_combine<3, true, EMU><<<g, blk, 0, s>>>(a); else k_weno_combine<3, false, EMU><<<g, blk, 0, s>>>(a); break;
+  }
 }
 
 }  // namespace
