@@ -242,10 +242,7 @@ struct AdjAxisArgs {
   int nseg;
 };
 
-// one out-of-line copy of the integer-pipe division (instruction footprint)
-__device__ __noinline__ double adj_div_outline(double a, double b) { return qss_emu::div(a, b); }
-
-template <int AX, bool OUT = false>
+template <int AX>
 __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
   const Box& b = a.b;
   int p, q, lo, hi;
@@ -334,8 +331,8 @@ __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
       const double S1 = Am_ + 0.25 * (b1t * b1t);
       const double S2 = A0_ + 0.25 * (e2 * e2);
       const double S3 = Ap_ + 0.25 * (b3t * b3t);
-      auto dv = [](double x, double y) { return OUT ? adj_div_outline(x, y) : qss_emu::div(x, y); };
-      const double r1 = dv(1.0, S1 + eps), r2 = dv(1.0, S2 + eps), r3 = dv(1.0, S3 + eps);
+      const double r1 = qss_emu::div(1.0, S1 + eps), r2 = qss_emu::div(1.0, S2 + eps),
+                   r3 = qss_emu::div(1.0, S3 + eps);
       // products of the weights on the integer pipes (the FP64 pipe bounds
       // this kernel, its integer pipes are ~90 % idle)
       using qss_emu::mul;
@@ -343,7 +340,7 @@ __global__ void __launch_bounds__(128) k_adj_axis(AdjAxisArgs a) {
       const double am2 = mul(0.6, q2);
       const double am1 = mul(0.1, q1), am3 = mul(0.3, q3);  // minus: 0.1, 0.6, 0.3
       const double ap1 = mul(0.3, q1), ap3 = mul(0.1, q3);  // plus (on S1, S2, S3): 0.3, 0.6, 0.1
-      const double iam = dv(1.0, am1 + am2 + am3), iap = dv(1.0, ap1 + am2 + ap3);
+      const double iam = qss_emu::div(1.0, am1 + am2 + am3), iap = qss_emu::div(1.0, ap1 + am2 + ap3);
       const double wm1 = mul(am1, iam), wm2 = mul(am2, iam), wm3 = mul(am3, iam);
       const double wp1 = mul(ap1, iap), wp2 = mul(am2, iap), wp3 = mul(ap3, iap);
       // candidate stencils: minus reads u0..u4, plus reads u4..u0
@@ -602,16 +599,6 @@ __global__ void k_scale_fill(Box b, const double* __restrict__ lam, double coef,
     const bool fill = i >= b.ilo && i <= b.ihi && j >= b.jlo && j <= b.jhi && k >= b.klo && k <= b.khi;
     wgt[p] = fill ? coef * lam[p] : 0.0;
   }
-}
-
-// $QSSGPU_ADJ_OUTLINE=1: the reverse window pass calls one out-of-line copy of
-// the integer-pipe division
-bool adj_outline() {
-  static const int on = [] {
-    const char* e = getenv("QSSGPU_ADJ_OUTLINE");
-    return e && atoi(e) == 1 ? 1 : 0;
-  }();
-  return on != 0;
 }
 
 unsigned g1(int64_t n) {
@@ -917,20 +904,17 @@ int adjoint_run(Options* o, QSS_DataArrays* p, Grid* g, const double* theta, con
       ax.bm = ar.bm[0];
       ax.inv = 1.0 / g->dx[0];
       ax.nseg = ns0;
-      if (adj_outline()) k_adj_axis<0, true><<<ag0, 128, 0, a.s>>>(ax);
-      else k_adj_axis<0, false><<<ag0, 128, 0, a.s>>>(ax);
+      k_adj_axis<0><<<ag0, 128, 0, a.s>>>(ax);
       ax.bp = ar.bp[1];
       ax.bm = ar.bm[1];
       ax.inv = 1.0 / g->dx[1];
       ax.nseg = ns1;
-      if (adj_outline()) k_adj_axis<1, true><<<ag1, 128, 0, a.s>>>(ax);
-      else k_adj_axis<1, false><<<ag1, 128, 0, a.s>>>(ax);
+      k_adj_axis<1><<<ag1, 128, 0, a.s>>>(ax);
       ax.bp = ar.bp[2];
       ax.bm = ar.bm[2];
       ax.inv = 1.0 / g->dx[2];
       ax.nseg = ns2;
-      if (adj_outline()) k_adj_axis<2, true><<<ag2, 128, 0, a.s>>>(ax);
-      else k_adj_axis<2, false><<<ag2, 128, 0, a.s>>>(ax);
+      k_adj_axis<2><<<ag2, 128, 0, a.s>>>(ax);
       k_adj_curv<<<g1(n), 256, 0, a.s>>>(b, cc, n, lam_in, coef_id, lam_out);
     };
     // recomputation of segment k's states from its checkpoint, on stream st
