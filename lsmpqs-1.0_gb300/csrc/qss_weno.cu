@@ -143,14 +143,12 @@ struct Centre {
 // three indicators of the plus side (S1+(c-2), S2+(c-1), S3+(c)) and of the
 // minus side (S1-(c+1), S2-(c), S3-(c-1)), each as first term + second term
 // in the reference's order of operations
-template <int EMU, bool SQ, bool OUTMUL = false>
+template <int EMU, bool SQ>
 __device__ __forceinline__ Centre make_centre(const Face& a, const Face& b, const Face& d) {
   using Q = Ar<EMU>;
-  // squares (and the 13/12 products) on the integer pipes when SQ, through
-  // one out-of-line product when OUTMUL
-  auto m2 = [](double x, double y) { return (OUTMUL && EMU >= 2) ? mul_outline(x, y) : Q::mul2(x, y); };
-  auto sq = [&](double t) { return SQ ? m2(t, t) : t * t; };
-  auto k13 = [&](double x) { return SQ ? m2(k1312, x) : k1312 * x; };
+  // squares (and the 13/12 products) on the integer pipes when SQ
+  auto sq = [](double t) { return SQ ? Q::mul2(t, t) : t * t; };
+  auto k13 = [](double x) { return SQ ? Q::mul2(k1312, x) : k1312 * x; };
   const double t2 = Q::s2(b.v, 1), t4 = Q::s2(b.v, 2);
   double t;
   t = (d.v - t2) + a.v;
@@ -508,7 +506,7 @@ __global__ void __launch_bounds__(G::NT, G::MB) k_weno_tile(AxisArgs a) {
     fb.v = sf[0][c + 1][line];
     fd.v = sf[0][c + 2][line];
     fd.t3 = sf[2][c + 2][line];
-    const Centre ct = make_centre<EMU, true, (MUL & 16) != 0>(fa, fb, fd);
+    const Centre ct = make_centre<EMU, true>(fa, fb, fd);
     sc[0][c][line] = ct.s1p;
     sc[1][c][line] = ct.s2p;
     sc[2][c][line] = ct.s3p;
@@ -767,12 +765,13 @@ void launch_tile_m(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int oth
 // tiles) / 192^3 (16 x 16): 0: 553.7 / 522.1, 2: 558.5 / 524.5,
 // 6: 580.8 / 546.1, 14: 592.4 / 539.4 (bit 0, the faces' squares and 3v on
 // the integer pipes: no gain; an out-of-line square root and division in the
-// combine kernel: none either).
+// combine kernel: none either; an out-of-line product in the centres' squares:
+// 578.7 / 539.1, a loss).
 int tile_mul() {
   static const int m = [] {
     const char* e = getenv("QSSGPU_TILE_MUL");
     const int v = e ? atoi(e) : -1;
-    return v == 0 || v == 2 || v == 6 || v == 14 || v == 22 || v == 30 ? v : -1;
+    return v == 0 || v == 2 || v == 6 || v == 14 ? v : -1;
   }();
   return m;
 }
@@ -783,8 +782,6 @@ void launch_tile(cudaStream_t s, int ax, const AxisArgs& a, int lanes, int other
     case 0: launch_tile_m<EMU, G, 0>(s, ax, a, lanes, other, along); break;
     case 2: launch_tile_m<EMU, G, 2>(s, ax, a, lanes, other, along); break;
     case 6: launch_tile_m<EMU, G, 6>(s, ax, a, lanes, other, along); break;
-    case 22: launch_tile_m<EMU, G, 22>(s, ax, a, lanes, other, along); break;
-    case 30: launch_tile_m<EMU, G, 30>(s, ax, a, lanes, other, along); break;
     default: launch_tile_m<EMU, G, 14>(s, ax, a, lanes, other, along); break;
   }
 }
