@@ -540,40 +540,24 @@ __global__ void __launch_bounds__(128) k_reinit_walk(Box b, const double* __rest
   int64_t c = b.idx(i, j, k0);
   double cc = __ldg(data + c);
   double dzm = scale(cc - __ldg(data + c - sz), inv.z);
-  // the loads of plane k are issued one plane ahead, so that they are in
-  // flight while plane k-1 is computed (the plane after the last one is
-  // still inside the ghost box: 3 ghost layers)
-  double xp = __ldg(data + c + 1), yp = __ldg(data + c + sy), zp = __ldg(data + c + sz);
-  double xo = li == 0 ? __ldg(data + c - 1) : 0.0, yo = lj == 0 ? __ldg(data + c - sy) : 0.0;
-  double p0 = __ldg(phi0 + c), d0 = __ldg(distance0 + c);
   for (int k = k0; k <= k1; k++) {
-    const int64_t cn = c + sz;
-    const double nxp = __ldg(data + cn + 1), nyp = __ldg(data + cn + sy), nzp = __ldg(data + cn + sz);
-    const double nxo = li == 0 ? __ldg(data + cn - 1) : 0.0, nyo = lj == 0 ? __ldg(data + cn - sy) : 0.0;
-    const double np0 = __ldg(phi0 + cn), nd0 = __ldg(distance0 + cn);
+    const double zp = __ldg(data + c + sz);
     double gp[3], gm[3];
-    gp[0] = scale(xp - cc, inv.x);
-    gp[1] = scale(yp - cc, inv.y);
+    gp[0] = scale(__ldg(data + c + 1) - cc, inv.x);
+    gp[1] = scale(__ldg(data + c + sy) - cc, inv.y);
     gp[2] = scale(zp - cc, inv.z);
     const double xm = __shfl_up_sync(0xffffffffu, gp[0], 1);
     const double ym = __shfl_up_sync(0xffffffffu, gp[1], 8);
-    gm[0] = li == 0 ? scale(cc - xo, inv.x) : xm;
-    gm[1] = lj == 0 ? scale(cc - yo, inv.y) : ym;
+    gm[0] = li == 0 ? scale(cc - __ldg(data + c - 1), inv.x) : xm;
+    gm[1] = lj == 0 ? scale(cc - __ldg(data + c - sy), inv.y) : ym;
     gm[2] = dzm;
     if (ok) {
-      const double r = reinit_rhs_diffs(cc, p0, d0, gp, gm, max_dx, far_bits);
-      next[c] = rhs_only ? r : cc + qss_emu::mul(dt_r, r);  // cc is data[c]
+      const double r = reinit_rhs_diffs(cc, phi0[c], distance0[c], gp, gm, max_dx, far_bits);
+      next[c] = rhs_only ? r : data[c] + qss_emu::mul(dt_r, r);
     }
     dzm = gp[2];
     cc = zp;
-    xp = nxp;
-    yp = nyp;
-    zp = nzp;
-    xo = nxo;
-    yo = nyo;
-    p0 = np0;
-    d0 = nd0;
-    c = cn;
+    c += sz;
   }
 }
 
