@@ -249,8 +249,9 @@ int qssgpu_axis_tuning_save(const char *path);
 /* adds the shapes of such a file to the table (a shape already there keeps
    its pick), so later processes in tuned mode (axis variant 2) skip the
    timing of those shapes; every line is checked first
-   (level 1-2, axis 0-2, positive sizes, form 0/1, 1 <= segment length <= line
-   length) and a file with any other line adds nothing; returns the number of
+   (level 1-2, axis 0-2, positive sizes, form 0 or 1 with 1 <= segment length
+   <= line length, form 3 with segment length 16, form 4 with segment length
+   27) and a file with any other line adds nothing; returns the number of
    shapes read, -1 on error */
 int qssgpu_axis_tuning_load(const char *path);
 /* Batched mode (no reference counterpart): the curvature ladder of
@@ -321,17 +322,6 @@ int qssgpu_forward_theta(Options *o, QSS_DataArrays *p, Grid *g, const double *t
    by binade-wise integer sums for non-negative runs, element by element
    elsewhere; the volume integrals use the same code.  0 on success. */
 int qssgpu_loop_sum(const double *values, long long n, double *out);
-/* Device self-test of the integer-pipe FP64 arithmetic against the native
-   instructions on n generated operand pairs: counts[0..7] = mismatches of
-   div, mul, add, sub, scale2, comparisons, max, sqrt; counts[8] = cases run
-   (counts holds 9 values); first = {operation, x, y} of one mismatch (may
-   be NULL). */
-int qssgpu_emu_selftest(long long n, unsigned long long seed, long long *counts, double *first);
-/* Throughput (G operations/s) of native / emulated division, multiplication
-   and addition: out[0..5] = div native, div emulated, mul native, mul
-   emulated, add native, add emulated; out[6] = multiplications with half
-   of the chains native and half emulated (out holds 7 doubles). */
-int qssgpu_op_rates(double *out);
 int qssgpu_get_slabs(const Grid *g);
 /* frees the device copy kept for p (destroyQSSDataArrays calls it) */
 void qssgpu_release(QSS_DataArrays *p);
@@ -355,17 +345,6 @@ void qssgpu_call_times(const QSS_DataArrays *p, const Grid *g, double *out);
    as in qssgpu_call_times, out[0] their sum (out holds 8 doubles); waits for
    the recorded events */
 void qssgpu_call_device_times(const QSS_DataArrays *p, const Grid *g, double *out);
-/* benchmark support: drain_model3d's set-up for curvature a0 with the arrays
-   left in HBM, then timing of `steps` inner steps after `warmup`
-   (out[0] total ms, out[1] mean ms per launch of the stage kernel with the
-   largest total time, out[2] kernels per step, out[3] ms inside stage
-   kernels, out[4] kind of that kernel: 0 fused stage, 1/2/3 WENO5 x/y/z
-   pass, 4 WENO5 combine; out[5..9] ms and out[10..14] launches per kind;
-   out holds 15 doubles); FP64 throughput probe (TFLOP/s of DFMA, DADD) */
-int qssgpu_prepare_step(Options *o, QSS_DataArrays *p, Grid *g, double a0);
-int qssgpu_time_steps(Options *o, QSS_DataArrays *p, Grid *g, double a0, int warmup, int steps,
-                      double *out);
-int qssgpu_fp64_peak(double *out);
 
 /* Allocation-free smoothed volume of {phi < 0} (no counterpart in the
    reference; same result, bit for bit, as qss3dvolumeregionphilessthanzero_).
@@ -393,6 +372,31 @@ int qssgpu_fp64_peak(double *out);
    code (see qssgpu_last_error). */
 int qssgpu_volume_noalloc(const double *d_phi, const int gb[6], const int ib[6], double dx, double dy,
                           double dz, double epsilon, double *d_volume, void *stream);
+
+/* ---------------- diagnostics and benchmark support ---------------------- */
+/* Measurement tools, not part of the path: nothing above calls them. */
+/* Device self-test of the integer-pipe FP64 arithmetic against the native
+   instructions on n generated operand pairs: counts[0..7] = mismatches of
+   div, mul, add, sub, scale2, comparisons, max, sqrt; counts[8] = cases run
+   (counts holds 9 values); first = {operation, x, y} of one mismatch (may
+   be NULL). */
+int qssgpu_emu_selftest(long long n, unsigned long long seed, long long *counts, double *first);
+/* Throughput (G operations/s) of native / emulated division, multiplication
+   and addition: out[0..5] = div native, div emulated, mul native, mul
+   emulated, add native, add emulated; out[6] = multiplications with half
+   of the chains native and half emulated (out holds 7 doubles). */
+int qssgpu_op_rates(double *out);
+/* benchmark support: drain_model3d's set-up for curvature a0 with the arrays
+   left in HBM, then timing of `steps` inner steps after `warmup`
+   (out[0] total ms, out[1] mean ms per launch of the stage kernel with the
+   largest total time, out[2] kernels per step, out[3] ms inside stage
+   kernels, out[4] kind of that kernel: 0 fused stage, 1/2/3 WENO5 x/y/z
+   pass, 4 WENO5 combine; out[5..9] ms and out[10..14] launches per kind;
+   out holds 15 doubles); FP64 throughput probe (TFLOP/s of DFMA, DADD) */
+int qssgpu_prepare_step(Options *o, QSS_DataArrays *p, Grid *g, double a0);
+int qssgpu_time_steps(Options *o, QSS_DataArrays *p, Grid *g, double a0, int warmup, int steps,
+                      double *out);
+int qssgpu_fp64_peak(double *out);
 
 #ifdef __cplusplus
 }
