@@ -636,11 +636,31 @@ def adjoint_arm(args):
                                 ckpt, C.byref(loss), Q.dptr(grad)):
         Q.check(lib)
     t_adj = time.perf_counter() - t0
+    # the same gradient with the whole trajectory kept in HBM (one segment:
+    # no recomputation; ~85 GB at 128^3 / 200 steps); the gradient does not
+    # depend on the checkpoint spacing, bit for bit
+    store_all = None
+    if args.adj_store_all:
+        grad1 = np.zeros(v["mask"].shape)
+        loss1 = C.c_double(0)
+        t0 = time.perf_counter()
+        rc = lib.qssgpu_adjoint_theta(C.byref(o), C.byref(v.p), C.byref(g), Q.dptr(theta), Q.dptr(target), steps,
+                                      dt, 0, C.byref(loss1), Q.dptr(grad1))
+        t_all = time.perf_counter() - t0
+        if rc:
+            store_all = {"error": lib.qssgpu_error_string().decode(errors="replace")}
+            lib.qssgpu_clear_error()
+        else:
+            store_all = {"forward_and_gradient_s": t_all, "adjoint_cost_over_forward": t_all / t_fwd,
+                         "gradient_equals_checkpointed": bool(np.array_equal(grad1, grad)),
+                         "note": "checkpoint_every = steps: every stage state and WENO5 derivative of the "
+                                 "forward pass kept in HBM, so the backward pass is the reverse sweep alone"}
     return {"n": n, "steps": steps, "checkpoint_every": ckpt, "loss": loss.value,
             "forward_s": t_fwd, "forward_and_gradient_s": t_adj, "adjoint_cost_over_forward": t_adj / t_fwd,
             "backward_over_forward": (t_adj - t_fwd) / t_fwd,
             "forward_voxel_steps_per_s": n ** 3 * steps / t_fwd,
             "grad_abs_max": float(np.abs(grad).max()),
+            "store_all": store_all,
             "note": "wall clock including uploads; adjoint_cost_over_forward = (forward + gradient) / forward, "
                     "backward_over_forward = the backward pass (checkpoint recomputation + reverse sweep) / "
                     "forward; gradient d loss / d theta per voxel (radians)"}
@@ -760,6 +780,8 @@ def main():
     ap.add_argument("--adj-n", type=int, default=128)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-ckpt", type=int, default=20)
+    ap.add_argument("--no-adj-store-all", dest="adj_store_all", action="store_false",
+                    help="skip the adjoint run that keeps the whole trajectory in HBM (no recomputation)")
     ap.add_argument("--axis-variant", type=int, default=None,
                     help="WENO5 axis passes: 0 registers, 1 shared memory, 2 launch shapes tuned by timing, "
                          "3 tiles with one voxel per thread (default: tiles)")

@@ -642,18 +642,31 @@ struct StageDerivs {
 struct SegBufs {
   std::vector<double*> sphi, ss1, ss2, ss3;
   std::vector<StageDerivs> sder;
+  // one allocation for the whole segment (4 states and, with derivs, 18
+  // derivative arrays per step, each starting on a 256-byte boundary): a
+  // trajectory kept whole at 128^3 / 200 steps is 4400 arrays, and a
+  // cudaMalloc / cudaFree pair per array (cudaFree synchronises the device)
+  // is host time the GPU waits through
   void alloc(DBufs& buf, int steps, int64_t n, bool derivs) {
+    const int64_t pitch = (n + 31) / 32 * 32;
+    const int64_t per_step = 4 + (derivs ? 18 : 0);
+    double* slab = buf.get(pitch * per_step * steps);
+    auto next = [&]() {
+      double* p = slab;
+      slab += pitch;
+      return p;
+    };
     for (int q = 0; q < steps; q++) {
-      sphi.push_back(buf.get(n));
-      ss1.push_back(buf.get(n));
-      ss2.push_back(buf.get(n));
-      ss3.push_back(buf.get(n));
+      sphi.push_back(next());
+      ss1.push_back(next());
+      ss2.push_back(next());
+      ss3.push_back(next());
     }
     if (derivs) {
       sder.resize(steps);
       for (auto& sd : sder)
         for (int st = 0; st < 3; st++)
-          for (int c = 0; c < 6; c++) sd.d[st][c] = buf.get(n);
+          for (int c = 0; c < 6; c++) sd.d[st][c] = next();
     }
   }
   const StageDerivs* keep(int q) const { return sder.empty() ? nullptr : &sder[q]; }
