@@ -7,8 +7,8 @@ one portable evaluation instead, so that they agree bit for bit on every
 machine.  These tests bound what that changes, against the oracle built with
 libm's sin/cos (oracle/liboracle_libm.so):
 
-* the level set after every curvature step within 1e-10 (the north-star
-  bound), the connectivity labels and the binary image identical, the
+* the level set after every curvature step within 1e-10 (the parity bound
+  of the path), the connectivity labels and the binary image identical, the
   trapped-phase masks with identical trapped sets and values within 1e-10,
   and the wetting saturation (each side's volume of phi < 0 over its volume
   of the pore space) within 1e-12;
